@@ -1,0 +1,233 @@
+"""ctypes wrapper around the CPU oracle (oracle/librapt_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py``, always as the checker or the timed CPU
+baseline, never as part of the product path.
+
+The oracle restates RAPT's hot path (rapt/fields.py, rapt/Particle.py,
+rapt/GuidingCenter.py, rapt/Adaptive.py, rapt/utils.py, rapt/rkf.py and the
+SciPy ``ode`` dopri5/dop853 drivers the reference calls). Its agreement with the
+reference itself is pinned by tests/test_oracle.py against fixtures written by
+tests/golden/make_golden.py.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librapt_oracle.so")
+
+FIELD_IDS = {
+    "EarthDipole": 0, "DoubleDipole": 1, "UniformBz": 2, "UniformCrossedEB": 3,
+    "VarEarthDipole": 4, "Parabolic": 5, "Harris": 6, "CompressedDipole": 7,
+}
+
+ST = dict(OK=0, MAXSTEPS=2, HMIN=3, NONFINITE=4, GC_NOCONV=5, ROWS_FULL=6, BAD_INPUT=7,
+          RKF_HMIN=8, ADAPTIVE_LIMIT=9)
+
+
+class Field(C.Structure):
+    _fields_ = [("model", C.c_int), ("is_static", C.c_int), ("p", C.c_double * 8),
+                ("gradstep", C.c_double), ("timestep", C.c_double)]
+
+
+class Config(C.Structure):
+    _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("cycres", C.c_double),
+                ("gctimestep", C.c_double), ("epss", C.c_double), ("epst", C.c_double),
+                ("enforce_equatorial", C.c_int), ("tableau", C.c_int), ("gc_eom", C.c_int),
+                ("nsteps", C.c_int), ("rkf_tol", C.c_double), ("rkf_hmin", C.c_double)]
+
+
+TRACER_DTYPE = np.dtype([
+    ("mode", "i4"), ("status", "i4"), ("t", "f8"), ("s", "f8", 6), ("mu", "f8"), ("v", "f8"),
+    ("mass", "f8"), ("charge", "f8"), ("tcur", "f8"), ("naccept", "i8"), ("nreject", "i8"),
+    ("nfcn", "i8"), ("nstep", "i8")], align=True)
+
+
+class Tracer(C.Structure):
+    _fields_ = [("mode", C.c_int), ("status", C.c_int), ("t", C.c_double), ("s", C.c_double * 6),
+                ("mu", C.c_double), ("v", C.c_double), ("mass", C.c_double),
+                ("charge", C.c_double), ("tcur", C.c_double), ("naccept", C.c_int64),
+                ("nreject", C.c_int64), ("nfcn", C.c_int64), ("nstep", C.c_int64)]
+
+
+assert C.sizeof(Tracer) == TRACER_DTYPE.itemsize
+
+_lib = None
+_P = C.POINTER
+_d = C.c_double
+_dp = _P(C.c_double)
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        F, Cf, T = _P(Field), _P(Config), _P(Tracer)
+        sig = {
+            "orc_field_init": (None, [F, C.c_int, _dp, C.c_int]),
+            "orc_config_default": (None, [Cf]),
+            "orc_B": (None, [F, _dp, _dp]), "orc_E": (None, [F, _dp, _dp]),
+            "orc_magB": (_d, [F, _dp]), "orc_unitb": (None, [F, _dp, _dp]),
+            "orc_gradB": (None, [F, _dp, _dp]), "orc_jacobianB": (None, [F, _dp, _dp]),
+            "orc_curvature": (_d, [F, _dp]), "orc_curlb": (None, [F, _dp, _dp]),
+            "orc_dBdt": (_d, [F, _dp]), "orc_dbdt": (None, [F, _dp, _dp]),
+            "orc_lengthscale": (_d, [F, _dp]), "orc_timescale": (_d, [F, _dp]),
+            "orc_particle_rhs": (None, [F, Cf, _d, _d, _d, _d, _dp, _dp]),
+            "orc_gc_rhs": (None, [F, Cf, C.c_int, _d, _d, _d, _d, _d, _dp, _dp]),
+            "orc_integrate_particle": (C.c_int, [F, Cf, C.c_int, _d, _d, _d, _dp, _dp, _d, _d,
+                                                 _P(C.c_int64)]),
+            "orc_integrate_gc": (C.c_int, [F, Cf, C.c_int, _d, _d, _d, _d, _dp, _dp, _d,
+                                           _P(C.c_int64)]),
+            "orc_particle_new": (None, [_dp, _dp, _d, _d, _d, T]),
+            "orc_gc_new_pa": (None, [F, _dp, _d, _d, _d, _d, _d, T]),
+            "orc_guidingcenter": (C.c_int, [F, _d, _dp, _dp, _d, _d, _dp, _dp, _dp]),
+            "orc_gctofp": (None, [F, _d, _dp, _d, _d, _d, _d, _d, _dp, _dp]),
+            "orc_gc_from_particle": (C.c_int, [F, T, T]),
+            "orc_particle_from_gc": (None, [F, T, T]),
+            "orc_particle_isadiabatic": (C.c_int, [F, Cf, T]),
+            "orc_gc_isadiabatic": (C.c_int, [F, Cf, T]),
+            "orc_particle_advance": (C.c_int, [F, Cf, T, _d, C.c_int, _dp, C.c_int, _P(C.c_int)]),
+            "orc_gc_advance": (C.c_int, [F, Cf, T, _d, C.c_int, _dp, C.c_int, _P(C.c_int)]),
+            "orc_adaptive_init": (C.c_int, [F, Cf, _dp, _dp, _d, _d, _d, T]),
+            "orc_adaptive_advance": (C.c_int, [F, Cf, T, _d, _dp, _P(C.c_int8), C.c_int,
+                                               _P(C.c_int), _dp, _P(C.c_int8), C.c_int,
+                                               _P(C.c_int)]),
+            "orc_batch_advance": (None, [F, Cf, C.c_int, C.c_int64, C.c_void_p, _dp, C.c_int]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _vec(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if n is not None:
+        assert a.size == n
+    return a, a.ctypes.data_as(_dp)
+
+
+def field(name_or_id, params=()):
+    """Build an oracle field struct; ``params`` override the model defaults in order."""
+    mid = FIELD_IDS[name_or_id] if isinstance(name_or_id, str) else int(name_or_id)
+    f = Field()
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    lib().orc_field_init(C.byref(f), mid, p.ctypes.data_as(_dp), len(p))
+    return f
+
+
+def config(rtol=1.49012e-8, atol=1.49012e-8, cycres=10, gctimestep=0.0, epss=5e-2, epst=5e-2,
+           enforce_equatorial=False, tableau=0, gc_eom=0, nsteps=500, rkf_tol=1e-3,
+           rkf_hmin=1e-12):
+    c = Config()
+    lib().orc_config_default(C.byref(c))
+    c.rtol, c.atol, c.cycres, c.gctimestep = rtol, atol, cycres, gctimestep
+    c.epss, c.epst, c.enforce_equatorial = epss, epst, int(bool(enforce_equatorial))
+    c.tableau, c.gc_eom, c.nsteps, c.rkf_tol, c.rkf_hmin = tableau, gc_eom, nsteps, rkf_tol, rkf_hmin
+    return c
+
+
+def field_eval(f, what, tpos):
+    """Evaluate one _Field quantity at a (t,x,y,z) point."""
+    L = lib()
+    tp, ptp = _vec(tpos, 4)
+    if what in ("magB", "curvature", "dBdt", "lengthscale", "timescale"):
+        return getattr(L, "orc_" + what)(C.byref(f), ptp)
+    n = 9 if what == "jacobianB" else 3
+    out = np.zeros(n)
+    getattr(L, "orc_" + what)(C.byref(f), ptp, out.ctypes.data_as(_dp))
+    return out.reshape(3, 3) if n == 9 else out
+
+
+def particle_rhs(f, cfg, mass, charge, gm, t, Y):
+    Y, pY = _vec(Y, 6)
+    out = np.zeros(6)
+    lib().orc_particle_rhs(C.byref(f), C.byref(cfg), mass, charge, gm, t, pY, out.ctypes.data_as(_dp))
+    return out
+
+
+def gc_rhs(f, cfg, mass, charge, mu, v, t, Y, eom=0):
+    Y, pY = _vec(Y, 4)
+    out = np.zeros(4)
+    lib().orc_gc_rhs(C.byref(f), C.byref(cfg), eom, mass, charge, mu, v, t, pY,
+                     out.ctypes.data_as(_dp))
+    return out
+
+
+def particle_new(pos, vel, t0, mass, charge):
+    tr = Tracer()
+    p, pp = _vec(pos, 3)
+    v, pv = _vec(vel, 3)
+    lib().orc_particle_new(pp, pv, t0, mass, charge, C.byref(tr))
+    return tr
+
+
+def gc_new_pa(f, pos, v, pa, t0, mass, charge):
+    tr = Tracer()
+    p, pp = _vec(pos, 3)
+    lib().orc_gc_new_pa(C.byref(f), pp, v, pa, t0, mass, charge, C.byref(tr))
+    return tr
+
+
+def tracer_to_dict(tr):
+    return {k: (list(getattr(tr, k)) if k == "s" else getattr(tr, k)) for k, _ in Tracer._fields_}
+
+
+def advance(f, cfg, tr, delta, check=False, max_rows=100000):
+    """Advance one Particle/GC tracer; returns (raised, rows[n,7])."""
+    rows = np.zeros((max_rows, 7))
+    n = C.c_int(0)
+    fn = lib().orc_particle_advance if tr.mode == 0 else lib().orc_gc_advance
+    raised = fn(C.byref(f), C.byref(cfg), C.byref(tr), delta, int(check),
+                rows.ctypes.data_as(_dp), max_rows, C.byref(n))
+    return raised, rows[: min(n.value, max_rows)].copy()
+
+
+def adaptive_init(f, cfg, pos, vel, t0, mass, charge):
+    tr = Tracer()
+    p, pp = _vec(pos, 3)
+    v, pv = _vec(vel, 3)
+    lib().orc_adaptive_init(C.byref(f), C.byref(cfg), pp, pv, t0, mass, charge, C.byref(tr))
+    return tr
+
+
+def adaptive_advance(f, cfg, tr, delta, max_rows=200000, max_sw=10000):
+    rows = np.zeros((max_rows, 7))
+    rmode = np.zeros(max_rows, dtype=np.int8)
+    swt = np.zeros(max_sw)
+    swm = np.zeros(max_sw, dtype=np.int8)
+    n, ns = C.c_int(0), C.c_int(0)
+    rc = lib().orc_adaptive_advance(
+        C.byref(f), C.byref(cfg), C.byref(tr), delta, rows.ctypes.data_as(_dp),
+        rmode.ctypes.data_as(_P(C.c_int8)), max_rows, C.byref(n), swt.ctypes.data_as(_dp),
+        swm.ctypes.data_as(_P(C.c_int8)), max_sw, C.byref(ns))
+    k, m = min(n.value, max_rows), min(ns.value, max_sw)
+    return rc, rows[:k].copy(), rmode[:k].copy(), swt[:m].copy(), swm[:m].copy()
+
+
+def batch_advance(f, cfg, kind, tracers, delta, nthreads=None):
+    """Advance a structured array of TRACER_DTYPE in place (kind 0 P, 1 GC, 2 Adaptive)."""
+    assert tracers.dtype == TRACER_DTYPE and tracers.flags.c_contiguous
+    d = np.ascontiguousarray(np.broadcast_to(np.asarray(delta, np.float64), tracers.shape))
+    nthreads = nthreads or os.cpu_count()
+    lib().orc_batch_advance(C.byref(f), C.byref(cfg), kind, tracers.size, tracers.ctypes.data,
+                            d.ctypes.data_as(_dp), nthreads)
+    return tracers
+
+
+def tracers_from_structs(structs):
+    arr = np.zeros(len(structs), dtype=TRACER_DTYPE)
+    for i, s in enumerate(structs):
+        C.memmove(arr[i:i + 1].ctypes.data, C.byref(s), C.sizeof(Tracer))
+    return arr
