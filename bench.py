@@ -1,0 +1,271 @@
+#!/usr/bin/env python3
+"""Benchmark: accepted RK steps/s of the 1M-tracer guiding-centre ensemble.
+
+Workload (``gc_doubledipole_1M``): 1,048,576 electrons in the double-dipole
+field, config-2 distributions (L 4-7, MLT 0-24 h, KE log-uniform 0.1-10 MeV,
+equatorial pitch 15-85 deg, seed 0), Tao-Chan-Brizard guiding-centre
+equations, DOPRI5 at rtol = atol = 1e-8, GCtimestep 1 s. One step = one
+``GuidingCenter.advance(1.0)`` of every tracer (one output interval).
+
+``value`` is whole-job accepted steps / device time with the state resident in
+HBM; ``e2e`` is the same metric through the public API with the state copied
+from pinned host memory and back inside the timed region. ``--impl reference``
+times the CPU restatement of the reference algorithm (the oracle) on all host
+cores over a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "accepted RK steps/s at 1M particles, learned+FP32 vs plain FP64 GPU at rtol 1e-8"
+UNIT = "accepted steps/s"
+
+# Algorithmic FP64 work of one accepted DOPRI5 step of the Tao-Chan-Brizard
+# guiding-centre equations in the double-dipole field: 6 right-hand sides of
+# 446 flops (7-point stencil of 7 B evaluations) + 275 flops of stage
+# combination, error norm and control; rsqrt/sqrt/div/pow count as one flop each.
+FLOPS_PER_ACCEPTED_STEP = 6 * 446 + 275 + 6 * 23 + 4
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1 << 20, help="tracers per GPU")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="tracers in the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        return rank, ws, dist
+    return 0, 1, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.p is None:
+            return out
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except Exception:
+            self.p.kill()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if sm:
+            hi = [s for s in sm if s > 0.5 * max(sm)] or sm
+            out = {"sm_mhz": statistics.median(hi), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def cpu_baseline(n_sample, threads):
+    """The oracle (CPU restatement of the reference algorithm) on host cores."""
+    from oracle import oracle as O
+    from rapt_gb300 import workloads as W
+    w = W.gc_bench(1 << 20)
+    idx = np.linspace(0, len(w["mass"]) - 1, n_sample).astype(np.int64)
+    w = W.subsample(w, idx)
+    f = O.field("DoubleDipole")
+    cfg = O.config(rtol=1e-8, atol=1e-8, gctimestep=1.0)
+    tr = O.tracers_from_structs([O.gc_new_pa(f, w["pos"][i], w["v"][i], w["pa"][i], 0.0, w["mass"][i],
+                                             w["charge"][i]) for i in range(n_sample)])
+    t = time.perf_counter()
+    O.batch_advance(f, cfg, 1, tr, 1.0, nthreads=threads)
+    dt = time.perf_counter() - t
+    acc = int(tr["naccept"].sum())
+    return acc / dt, acc, dt
+
+
+def run_reference(args, rank, ws, dist):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n = args.cpu_sample or 4096
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, acc, dt = cpu_baseline(n, threads)
+        if i >= args.warmup:
+            vals.append((acc, dt))
+    acc = sum(a for a, _ in vals)
+    dt = sum(d for _, d in vals)
+    value = acc / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded, config-2 distributions)",
+            "config": {"workload": "gc_doubledipole_1M", "sample_tracers_per_step": n,
+                       "step": "GuidingCenter.advance(1.0) of each sampled tracer"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d of the 1,048,576 tracers (evenly spaced), 1 s each" % n},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, ws, dist):
+    from rapt_gb300 import Ensemble, workloads as W, fields as F
+    from rapt_gb300 import _native as N
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx = N.Context(dev)
+    w = W.gc_bench(args.n, seed=rank)
+    n = len(w["mass"])
+    ens = Ensemble(F.DoubleDipole(), n, max_rows=4, ctx=ctx, pinned=not args.no_e2e)
+    ens.configure(**w["params"])
+    ens.set_guiding_centers(w["pos"], w["v"], pa=w["pa"], t0=0.0, mass=w["mass"], charge=w["charge"])
+    init = {k: (v.copy()) for k, v in ens.h.items()}
+    ens.upload()
+    fp64_peak, fp32_peak = ctx.measure_peaks()
+
+    for _ in range(args.warmup):
+        ens.advance("gc", 1.0)
+        ens.rows(reset=True)
+    # ---- device-resident timed region
+    barrier(dist)
+    clk = Clocks(dev) if rank == 0 else None
+    t0 = time.perf_counter()
+    acc = 0
+    dev_ms = 0.0
+    launches = 0
+    for _ in range(args.steps):
+        st = ens.advance("gc", 1.0)
+        acc += st["accepted"]
+        dev_ms += st["kernel_ms"]
+        launches += st["kernel_launches"]
+        ens.ctx.check(ens.ctx.L.rapt_rows_download(ens.ctx.h, None, None, None, None, None, 1), "reset rows")
+    wall = time.perf_counter() - t0
+    clocks = clk.stop() if clk else None
+    barrier(dist)
+    dev_s = allmax(dist, dev_ms * 1e-3)
+    acc_all = allsum(dist, acc)
+    value = acc_all / dev_s
+    # ---- end to end through the public API with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        for k, v in init.items():
+            ens.h[k][...] = v
+        h2d = sum(ens.h[k].nbytes for k in ens.h)
+        d2h = h2d + n * ens.max_rows * 8 * 8  # state back + rows buffer
+        barrier(dist)
+        t1 = time.perf_counter()
+        acc_e = 0
+        for _ in range(args.steps):
+            ens.upload()
+            st = ens.advance("gc", 1.0)
+            acc_e += st["accepted"]
+            ens.download()
+            ens.rows(reset=True)
+        e2e_s = allmax(dist, time.perf_counter() - t1)
+        e2e = {"value": allsum(dist, acc_e) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+    if rank != 0:
+        return
+    achieved = FLOPS_PER_ACCEPTED_STEP * acc / (dev_ms * 1e-3) / 1e12
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded, config-2 distributions at 2^20 tracers per GPU)",
+            "config": {"workload": "gc_doubledipole_1M", "tracers_per_gpu": n, "form": "plain",
+                       "eom": "TaoChanBrizard", "method": "DOPRI5", "rtol": 1e-8, "atol": 1e-8,
+                       "step": "GuidingCenter.advance(1.0) of every tracer",
+                       "l2": "state 1M x 232 B > L2 (compute bound; no flush)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp64_peak, "traffic": None,
+                         "peak_source": "measured in-run: FP64 FMA chains (rapt_measure_peaks)",
+                         "flops_per_accepted_step": FLOPS_PER_ACCEPTED_STEP, "fp32_peak_tflops": fp32_peak},
+            "gpu_launches": int(launches), "clocks": clocks, "wall_s": wall}
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu_baseline:
+        n_s = args.cpu_sample or 4096
+        v, a, dt = cpu_baseline(n_s, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": "%d of the 1,048,576 tracers, 1 s each (%.1f s)" % (n_s, dt)}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, ws, dist = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, rank, ws, dist)
+    else:
+        run_ours(args, rank, ws, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

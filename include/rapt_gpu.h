@@ -1,0 +1,196 @@
+/*
+ * rapt_gpu.h -- C ABI of librapt_gpu.so, the GB300 ensemble tracer.
+ *
+ * RAPT (mkozturk/rapt) has no FFI: its boundary is the Python class API
+ * (Particle, GuidingCenter, Adaptive, rapt.params, the field objects). This
+ * header is the layer that a Python facade with the same classes binds through
+ * ctypes; each entry point names the reference interface it stands in for.
+ *
+ * Conventions
+ *  - Every call returns an int: RAPT_OK (0) or an RAPT_ERR_* code. The text of
+ *    the last error of a context is returned by rapt_last_error().
+ *  - Host buffers are owned by the caller (C-contiguous, float64 unless stated).
+ *    The context owns all device memory.
+ *  - One context per host thread; calls on one context are not thread-safe.
+ *  - Kernels never trap: per-tracer failures come back in the status array.
+ */
+#ifndef RAPT_GPU_H
+#define RAPT_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RAPT_GPU_ABI_VERSION 1
+
+/* Return codes. */
+enum {
+  RAPT_OK = 0,
+  RAPT_ERR_INVALID = 1,     /* bad argument */
+  RAPT_ERR_CUDA = 2,        /* CUDA runtime error */
+  RAPT_ERR_NOMEM = 3,       /* device allocation failed */
+  RAPT_ERR_UNSUPPORTED = 4, /* e.g. field model without a device implementation */
+  RAPT_ERR_STATE = 5        /* call out of order (no ensemble, no field, ...) */
+};
+
+/* Field models with a device implementation (rapt/fields.py). */
+enum {
+  RAPT_EARTH_DIPOLE = 0,       /* EarthDipole(B0)                 fields.py:282-317 */
+  RAPT_DOUBLE_DIPOLE = 1,      /* DoubleDipole(B0, distance, k)   fields.py:319-362 */
+  RAPT_UNIFORM_BZ = 2,         /* UniformBz(Bz)                   fields.py:364-390 */
+  RAPT_UNIFORM_CROSSED_EB = 3, /* UniformCrossedEB(Ey, Bz)        fields.py:392-427 */
+  RAPT_VAR_EARTH_DIPOLE = 4,   /* VarEarthDipole(amp, period)     fields.py:429-470 */
+  RAPT_PARABOLIC = 5,          /* Parabolic(B0, Bn, d)            fields.py:472-511 */
+  RAPT_HARRIS = 6,             /* Harris sheet (B0, L, Bn, Ey): no reference counterpart */
+  RAPT_COMPRESSED_DIPOLE = 7,  /* breathing dipole + induced E (B0, amp, period): no counterpart */
+  RAPT_N_MODELS = 8
+};
+
+/* Tracer modes and run kinds. */
+enum { RAPT_MODE_PARTICLE = 0, RAPT_MODE_GC = 1 };
+enum { RAPT_KIND_PARTICLE = 0, RAPT_KIND_GC = 1, RAPT_KIND_ADAPTIVE = 2 };
+
+/* Arithmetic forms. */
+enum {
+  RAPT_FORM_PLAIN = 0,        /* FP64 throughout, reference controller semantics */
+  RAPT_FORM_FP32 = 1,         /* FP32 stages, compensated accumulation, FP64 control */
+  RAPT_FORM_LEARNED = 2,      /* FP64 with MLP step proposals */
+  RAPT_FORM_LEARNED_FP32 = 3  /* FP32 stages with MLP step proposals */
+};
+
+/* Per-tracer status words. */
+enum {
+  RAPT_ST_OK = 0,
+  RAPT_ST_MAXSTEPS = 2,       /* SciPy idid -2: more than nsteps steps in one output interval */
+  RAPT_ST_HMIN = 3,           /* SciPy idid -3: step size too small */
+  RAPT_ST_NONFINITE = 4,      /* NaN/Inf in the state */
+  RAPT_ST_GC_NOCONV = 5,      /* utils.guidingcenter did not converge (reference returns None) */
+  RAPT_ST_ROWS_FULL = 6,      /* output row buffer full: drain rows and call again to resume */
+  RAPT_ST_BAD_INPUT = 7,      /* e.g. GCtimestep == 0 (bounce-period cadence not on device) */
+  RAPT_ST_RKF_HMIN = 8,       /* rkf.py RuntimeError at hmin */
+  RAPT_ST_ADAPTIVE_LIMIT = 9  /* adaptive segment cap reached */
+};
+
+/* Per-tracer flag bits (rapt_host_state.flags). */
+enum {
+  RAPT_FLAG_CHECK_ADIABATICITY = 1, /* tracer.check_adiabaticity */
+  RAPT_FLAG_RAISED = 2,             /* out: Adiabatic / NonAdiabatic was raised */
+  RAPT_FLAG_DONE = 4                /* internal: advance finished for this call */
+};
+
+/* Mirrors rapt.params (rapt/__init__.py:21-34) plus device options. */
+typedef struct {
+  double rtol, atol;             /* params["solvertolerances"] */
+  double cyclotronresolution;    /* params["cyclotronresolution"] */
+  double gctimestep;             /* params["GCtimestep"], must be > 0 */
+  double epss, epst;             /* params["epss"], params["epst"] */
+  int32_t enforce_equatorial;    /* params["enforce equatorial"] */
+  int32_t tableau;               /* 0: DOP853 particle / DOPRI5 GC (as the reference); 1: RKF45 (rkf.py) */
+  int32_t gc_eom;                /* 0 TaoChanBrizard, 1 BrizardChan, 2 NorthropTeller */
+  int32_t nsteps;                /* SciPy ode nsteps per output interval (500) */
+  double rkf_tol, rkf_hmin;      /* RKF45 tableau: rkf.py tol and hmin */
+  int32_t form;                  /* RAPT_FORM_* */
+  int32_t threads_per_block;     /* 0: default */
+  int64_t max_steps_per_launch;  /* per-thread RK-step budget of one launch (0: default) */
+  int32_t blocks_per_sm;         /* 0: default */
+  int32_t use_graph;             /* 1: replay the launch sequence as a captured CUDA graph */
+} rapt_config;
+
+/* Host-side SoA view of an ensemble. Any pointer may be NULL on download to
+ * skip that array. s[0..5]: particle x,y,z,px,py,pz; GC x,y,z,ppar,0,0. */
+typedef struct {
+  int64_t n;
+  int8_t* mode;        /* RAPT_MODE_* */
+  int32_t* status;     /* RAPT_ST_* */
+  int32_t* flags;      /* RAPT_FLAG_* */
+  double* t_int;       /* integrator time r.t */
+  double* t_row;       /* time of the last trajectory row (trajectory[-1,0]) */
+  double* tcur;        /* tracer.tcur */
+  double* s[6];
+  double* mu;          /* GC magnetic moment */
+  double* v;           /* GC speed attribute (GuidingCenter.v) */
+  double* mass;
+  double* charge;
+  int64_t* naccept;    /* accepted RK steps (SciPy NACCPT summed) */
+  int64_t* nreject;    /* rejected RK steps (NREJCT) */
+  int64_t* nfcn;       /* RHS evaluations as the reference counts them (NFCN) */
+  int32_t* nswitch;    /* Adaptive switches */
+} rapt_host_state;
+
+typedef struct {
+  int64_t accepted, rejected, rhs_evals, switches;
+  int64_t done, failed, launches, kernel_launches;
+  double kernel_ms;    /* device time of the advance, CUDA events on the context stream */
+} rapt_stats;
+
+/* --- context ------------------------------------------------------------ */
+int rapt_abi_version(void);
+/* Create a context on a CUDA device (its own stream). */
+int rapt_ctx_create(int device, void** ctx_out);
+void rapt_ctx_destroy(void* ctx);
+const char* rapt_last_error(const void* ctx);
+
+/* --- configuration ------------------------------------------------------- */
+/* Stand-in for passing a field object (rapt/fields.py) to a tracer. params
+ * override the model's constructor defaults in order. */
+int rapt_field_set(void* ctx, int model, const double* params, int nparams);
+/* Stand-in for assigning field.gradientstepsize / field.timederivstepsize
+ * (fields.py:38-41); call after rapt_field_set. */
+int rapt_field_set_steps(void* ctx, double gradientstepsize, double timederivstepsize);
+/* Stand-in for rapt.params (rapt/__init__.py:21-34). */
+void rapt_config_default(rapt_config* cfg);
+int rapt_config_set(void* ctx, const rapt_config* cfg);
+
+/* --- ensemble ------------------------------------------------------------ */
+/* Allocate device SoA storage for n tracers, max_rows output rows and
+ * max_switch switch-log entries per tracer. */
+int rapt_ensemble_alloc(void* ctx, int64_t n, int32_t max_rows, int32_t max_switch);
+/* Tracer construction state (Particle.__init__ Particle.py:59-109,
+ * GuidingCenter.__init__ GuidingCenter.py:63-133) copied host -> device. */
+int rapt_ensemble_upload(void* ctx, const rapt_host_state* h);
+int rapt_ensemble_download(void* ctx, rapt_host_state* h);
+/* Trajectory rows appended since the last reset (tracer.trajectory[1:]):
+ * rows[n][max_rows][7] = (t, s0..s5), row_mode[n][max_rows], nrows[n];
+ * switch log sw_time[n][max_switch], sw_mode[n][max_switch]. Any pointer may be
+ * NULL. reset != 0 empties the device row buffers afterwards. */
+int rapt_rows_download(void* ctx, double* rows, int8_t* row_mode, int32_t* nrows,
+                       double* sw_time, int8_t* sw_mode, int reset);
+
+/* --- advance ------------------------------------------------------------- */
+/* Particle.advance(delta)       Particle.py:230-309      kind RAPT_KIND_PARTICLE
+ * GuidingCenter.advance(delta)  GuidingCenter.py:397-458 kind RAPT_KIND_GC
+ * Adaptive.advance(delta)       Adaptive.py:187-222      kind RAPT_KIND_ADAPTIVE
+ * for every tracer of the ensemble at once. delta: per-tracer array (length n)
+ * or NULL to use delta_all. Returns when the device work has completed. */
+int rapt_advance(void* ctx, int kind, const double* delta, double delta_all, rapt_stats* stats);
+
+/* Adaptive.__init__ mode pick (Adaptive.py:70-104) on device: tracers given as
+ * particles are converted to guiding centres where Particle.isadiabatic() holds. */
+int rapt_adaptive_init(void* ctx);
+
+/* Single-point field evaluation for checks (fields.py _Field methods):
+ * what = 0 B, 1 E, 2 gradB, 3 curlb, 4 magB, 5 unitb, 6 lengthscale,
+ * 7 dbdt, 8 jacobianB (9 values), 9 dBdt, 10 timescale.
+ * tpos[n][4] host, out[n][9] host. */
+int rapt_field_eval(void* ctx, int what, int64_t n, const double* tpos, double* out);
+
+/* Right-hand sides at given states for checks (Particle.py:284-298,
+ * GuidingCenter.py:329-395). state[n][8] = (t, y0..y5, gm|mu), per-tracer
+ * mass/charge/v; out[n][6]. */
+int rapt_rhs_eval(void* ctx, int mode, int64_t n, const double* state, const double* mass,
+                  const double* charge, const double* v, double* out);
+
+/* Page-lock (pin) a caller-owned host buffer so that uploads and downloads
+ * through it run at full PCIe/NVLink-C2C speed; unregister before freeing. */
+int rapt_host_register(void* p, uint64_t bytes);
+int rapt_host_unregister(void* p);
+
+/* Measured FP64 and FP32 FMA throughput of this device (TFLOP/s), from a
+ * dependent-chain microkernel; used as roofline denominators. */
+int rapt_measure_peaks(void* ctx, double* fp64_tflops, double* fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RAPT_GPU_H */

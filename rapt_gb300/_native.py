@@ -1,0 +1,190 @@
+"""ctypes binding of librapt_gpu.so (declared in include/rapt_gpu.h).
+
+The library is built in-tree by ``rapt_gb300/build.py``. There is no CPU
+fallback: if the library is missing or no CUDA device is usable, the calls
+raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librapt_gpu.so")
+
+RAPT_OK, RAPT_ERR_INVALID, RAPT_ERR_CUDA, RAPT_ERR_NOMEM, RAPT_ERR_UNSUPPORTED, RAPT_ERR_STATE = range(6)
+MODEL_IDS = {"EarthDipole": 0, "DoubleDipole": 1, "UniformBz": 2, "UniformCrossedEB": 3,
+             "VarEarthDipole": 4, "Parabolic": 5, "Harris": 6, "CompressedDipole": 7}
+MODE_PARTICLE, MODE_GC = 0, 1
+KIND_PARTICLE, KIND_GC, KIND_ADAPTIVE = 0, 1, 2
+FORMS = {"plain": 0, "fp32": 1, "learned": 2, "learned_fp32": 3}
+ST = dict(OK=0, MAXSTEPS=2, HMIN=3, NONFINITE=4, GC_NOCONV=5, ROWS_FULL=6, BAD_INPUT=7,
+          RKF_HMIN=8, ADAPTIVE_LIMIT=9)
+FLAG_CHECK, FLAG_RAISED, FLAG_DONE = 1, 2, 4
+FIELD_QUANTITIES = {"B": 0, "E": 1, "gradB": 2, "curlb": 3, "magB": 4, "unitb": 5,
+                    "lengthscale": 6, "dbdt": 7, "jacobianB": 8, "dBdt": 9, "timescale": 10}
+
+
+class RaptConfig(C.Structure):
+    _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("cyclotronresolution", C.c_double),
+                ("gctimestep", C.c_double), ("epss", C.c_double), ("epst", C.c_double),
+                ("enforce_equatorial", C.c_int32), ("tableau", C.c_int32), ("gc_eom", C.c_int32),
+                ("nsteps", C.c_int32), ("rkf_tol", C.c_double), ("rkf_hmin", C.c_double),
+                ("form", C.c_int32), ("threads_per_block", C.c_int32),
+                ("max_steps_per_launch", C.c_int64), ("blocks_per_sm", C.c_int32),
+                ("use_graph", C.c_int32)]
+
+
+class RaptHostState(C.Structure):
+    _fields_ = [("n", C.c_int64), ("mode", C.c_void_p), ("status", C.c_void_p), ("flags", C.c_void_p),
+                ("t_int", C.c_void_p), ("t_row", C.c_void_p), ("tcur", C.c_void_p),
+                ("s", C.c_void_p * 6), ("mu", C.c_void_p), ("v", C.c_void_p), ("mass", C.c_void_p),
+                ("charge", C.c_void_p), ("naccept", C.c_void_p), ("nreject", C.c_void_p),
+                ("nfcn", C.c_void_p), ("nswitch", C.c_void_p)]
+
+
+class RaptStats(C.Structure):
+    _fields_ = [("accepted", C.c_int64), ("rejected", C.c_int64), ("rhs_evals", C.c_int64),
+                ("switches", C.c_int64), ("done", C.c_int64), ("failed", C.c_int64),
+                ("launches", C.c_int64), ("kernel_launches", C.c_int64), ("kernel_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# Every symbol include/rapt_gpu.h declares, with its ctypes signature.
+_VP, _D, _I, _I64 = C.c_void_p, C.c_double, C.c_int, C.c_int64
+_DP = C.POINTER(C.c_double)
+SIGNATURES = {
+    "rapt_abi_version": (C.c_int, []),
+    "rapt_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "rapt_ctx_destroy": (None, [_VP]),
+    "rapt_last_error": (C.c_char_p, [_VP]),
+    "rapt_field_set": (C.c_int, [_VP, C.c_int, _DP, C.c_int]),
+    "rapt_field_set_steps": (C.c_int, [_VP, _D, _D]),
+    "rapt_config_default": (None, [C.POINTER(RaptConfig)]),
+    "rapt_config_set": (C.c_int, [_VP, C.POINTER(RaptConfig)]),
+    "rapt_ensemble_alloc": (C.c_int, [_VP, _I64, C.c_int32, C.c_int32]),
+    "rapt_ensemble_upload": (C.c_int, [_VP, C.POINTER(RaptHostState)]),
+    "rapt_ensemble_download": (C.c_int, [_VP, C.POINTER(RaptHostState)]),
+    "rapt_rows_download": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int]),
+    "rapt_advance": (C.c_int, [_VP, C.c_int, _VP, _D, C.POINTER(RaptStats)]),
+    "rapt_adaptive_init": (C.c_int, [_VP]),
+    "rapt_field_eval": (C.c_int, [_VP, C.c_int, _I64, _VP, _VP]),
+    "rapt_rhs_eval": (C.c_int, [_VP, C.c_int, _I64, _VP, _VP, _VP, _VP, _VP]),
+    "rapt_measure_peaks": (C.c_int, [_VP, _DP, _DP]),
+    "rapt_host_register": (C.c_int, [_VP, C.c_uint64]),
+    "rapt_host_unregister": (C.c_int, [_VP]),
+}
+
+_lib = None
+
+
+class RaptError(RuntimeError):
+    pass
+
+
+def lib():
+    """Load librapt_gpu.so; raises ImportError if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("librapt_gpu.so is not built (run `python rapt_gb300/build.py`); "
+                              "rapt_gb300 has no CPU fallback")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def ctypes_byref(obj):
+    return C.byref(obj)
+
+
+class Context:
+    """One CUDA context + stream of the library (rapt_ctx_*)."""
+
+    def __init__(self, device=0):
+        self.L = lib()
+        h = C.c_void_p()
+        rc = self.L.rapt_ctx_create(int(device), C.byref(h))
+        if rc != RAPT_OK or not h.value:
+            raise RaptError("rapt_ctx_create(device=%d) failed with code %d (no usable CUDA device?)" % (device, rc))
+        self.h = h
+        self.device = device
+
+    def check(self, rc, what):
+        if rc != RAPT_OK:
+            msg = self.L.rapt_last_error(self.h)
+            raise RaptError("%s failed (code %d): %s" % (what, rc, msg.decode() if msg else ""))
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.L.rapt_ctx_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_field(self, model_id, params=(), gradientstepsize=None, timederivstepsize=None):
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        self.check(self.L.rapt_field_set(self.h, int(model_id), p.ctypes.data_as(_DP), len(p)), "rapt_field_set")
+        if gradientstepsize is not None or timederivstepsize is not None:
+            self.check(self.L.rapt_field_set_steps(self.h, float(gradientstepsize), float(timederivstepsize)),
+                       "rapt_field_set_steps")
+
+    def set_config(self, **kw):
+        cfg = RaptConfig()
+        self.L.rapt_config_default(C.byref(cfg))
+        for k, v in kw.items():
+            if v is None:
+                continue
+            if not hasattr(cfg, k):
+                raise KeyError(k)
+            setattr(cfg, k, v)
+        self.check(self.L.rapt_config_set(self.h, C.byref(cfg)), "rapt_config_set")
+        return cfg
+
+    def field_eval(self, quantity, tpos):
+        tpos = np.ascontiguousarray(np.atleast_2d(tpos), dtype=np.float64)
+        n = tpos.shape[0]
+        out = np.zeros((n, 9))
+        self.check(self.L.rapt_field_eval(self.h, FIELD_QUANTITIES[quantity], n, ptr(tpos), ptr(out)),
+                   "rapt_field_eval")
+        return out
+
+    def rhs_eval(self, mode, state, mass, charge, v=None):
+        state = np.ascontiguousarray(state, dtype=np.float64)
+        n = state.shape[0]
+        mass = np.ascontiguousarray(np.broadcast_to(mass, (n,)), dtype=np.float64)
+        charge = np.ascontiguousarray(np.broadcast_to(charge, (n,)), dtype=np.float64)
+        vv = None if v is None else np.ascontiguousarray(np.broadcast_to(v, (n,)), dtype=np.float64)
+        out = np.zeros((n, 6))
+        self.check(self.L.rapt_rhs_eval(self.h, int(mode), n, ptr(state), ptr(mass), ptr(charge), ptr(vv), ptr(out)),
+                   "rapt_rhs_eval")
+        return out
+
+    def measure_peaks(self):
+        a, b = C.c_double(), C.c_double()
+        self.check(self.L.rapt_measure_peaks(self.h, C.byref(a), C.byref(b)), "rapt_measure_peaks")
+        return a.value, b.value
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(int(os.environ.get("RAPT_DEVICE", "0")))
+    return _default_ctx

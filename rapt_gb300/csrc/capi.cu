@@ -1,0 +1,600 @@
+// capi.cu -- the C ABI of librapt_gpu.so (declared in include/rapt_gpu.h).
+//
+// The context owns one CUDA stream, one device block holding every SoA array
+// of the ensemble, and a small scratch block (work-queue heads and counters of
+// the persistent kernels). rapt_advance() runs rounds of one launch per mode
+// until no tracer is left pending (Adaptive alternates modes across rounds).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "launch.h"
+
+using namespace rapt;
+
+namespace {
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  bool field_set = false;
+  FieldP field{};
+  rapt_config cfg{};
+  int num_sms = 0;
+  int64_t n = 0;
+  int max_rows = 0, max_sw = 0;
+  void* block = nullptr;
+  DevEnsemble E{};
+  Scratch* scratch = nullptr;
+  unsigned long long* h_pending = nullptr;  // pinned
+  void* tmp = nullptr;
+  size_t tmp_bytes = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  ModelTable tab[RAPT_N_MODELS];
+};
+
+int fail(Ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess) return fail(c, RAPT_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+T* carve(char*& p, size_t count) {
+  T* r = reinterpret_cast<T*>(p);
+  size_t bytes = count * sizeof(T);
+  bytes = (bytes + 255) & ~size_t(255);
+  p += bytes;
+  return r;
+}
+
+size_t ensemble_bytes(int64_t n, int max_rows, int max_sw) {
+  auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  const size_t N = (size_t)n;
+  size_t b = 0;
+  b += 2 * al(N);                                      // mode, seg_active
+  b += al(N * max_rows) + al(N * max_sw);              // row_mode, sw_mode
+  b += 5 * al(N * 4);                                  // status, flags, nrows, nswitch, nseg
+  b += 19 * al(N * 8);                                 // doubles
+  b += al(N * max_rows * 7 * 8) + al(N * max_sw * 8);  // rows, sw_time
+  b += 3 * al(N * 8);                                  // int64 counters
+  return b;
+}
+
+void build_field(int model, const double* params, int np, FieldP* f) {
+  std::memset(f, 0, sizeof(*f));
+  f->model = model;
+  f->is_static = 1;
+  f->gradstep = 1e-6;  // _Field.__init__, fields.py:38-41
+  f->timestep = 1e-3;
+  double* p = f->p;
+  switch (model) {
+    case RAPT_EARTH_DIPOLE: p[0] = kB0; f->gradstep = kRe * 1e-6; break;
+    case RAPT_DOUBLE_DIPOLE: p[0] = kB0; p[1] = 20 * kRe; p[2] = 1; f->gradstep = kRe / 1000; break;
+    case RAPT_UNIFORM_BZ: p[0] = 1; break;
+    case RAPT_UNIFORM_CROSSED_EB: p[0] = 1; p[1] = 1; f->is_static = 0; break;
+    case RAPT_VAR_EARTH_DIPOLE: p[0] = 0.1; p[1] = 10; f->gradstep = kRe / 1000; f->is_static = 0; break;
+    case RAPT_PARABOLIC: p[0] = 10.0; p[1] = 1.0; p[2] = 0.2; break;
+    case RAPT_HARRIS: p[0] = 20e-9; p[1] = 0.5 * kRe; p[2] = 2e-9; p[3] = 0.2e-3; f->is_static = 0; break;
+    case RAPT_COMPRESSED_DIPOLE: p[0] = kB0; p[1] = 0.1; p[2] = 60.0; f->gradstep = kRe / 1000; f->is_static = 0; break;
+    default: break;
+  }
+  for (int i = 0; i < np && i < 8; ++i) p[i] = params[i];
+  if (model == RAPT_HARRIS) f->gradstep = p[1] * 1e-4;
+}
+
+void finish_field(FieldP* f) {
+  const double* p = f->p;
+  f->inv2d = 1.0 / (2.0 * f->gradstep);
+  switch (f->model) {
+    case RAPT_EARTH_DIPOLE: f->c0 = -3.0 * p[0] * kRe3; break;
+    case RAPT_DOUBLE_DIPOLE: f->c0 = -p[0] * kRe3; break;
+    case RAPT_VAR_EARTH_DIPOLE: f->c0 = -kB0 * kRe3; f->c1 = 2.0 * kPi / p[1]; break;
+    case RAPT_HARRIS: f->c0 = 1.0 / p[1]; break;
+    case RAPT_COMPRESSED_DIPOLE:
+      f->c0 = -p[0] * kRe3;
+      f->c1 = 2.0 * kPi / p[2];
+      f->c2 = p[0] * p[1] * f->c1 * kRe3;
+      break;
+    default: break;
+  }
+}
+
+KParams make_params(const Ctx* c, int kind) {
+  KParams P{};
+  P.f = c->field;
+  const rapt_config& g = c->cfg;
+  P.rtol = g.rtol; P.atol = g.atol; P.cycres = g.cyclotronresolution; P.gctimestep = g.gctimestep;
+  P.epss = g.epss; P.epst = g.epst; P.rkf_tol = g.rkf_tol; P.rkf_hmin = g.rkf_hmin;
+  P.enforce_eq = g.enforce_equatorial; P.tableau = g.tableau; P.gc_eom = g.gc_eom; P.nsteps = g.nsteps;
+  P.kind = kind; P.form = g.form;
+  P.budget = g.max_steps_per_launch > 0 ? g.max_steps_per_launch : (1LL << 62);
+  P.max_rows = c->max_rows; P.max_sw = c->max_sw;
+  P.max_segments = 100000;
+  return P;
+}
+
+__global__ void k_prepare(DevEnsemble E, const double* delta, double delta_all, int kind) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= E.n) return;
+  E.delta[k] = delta ? delta[k] : delta_all;
+  E.flags[k] &= RAPT_FLAG_CHECK_ADIABATICITY;
+  if (kind == RAPT_KIND_ADAPTIVE) E.flags[k] |= RAPT_FLAG_CHECK_ADIABATICITY;
+  E.seg_active[k] = 0;
+  E.nseg[k] = 0;
+  E.status[k] = RAPT_ST_OK;
+  E.t_int[k] = E.t_row[k];
+}
+
+__global__ void k_fill_defaults(DevEnsemble E, int have_tint, int have_tcur) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= E.n) return;
+  if (!have_tint) E.t_int[k] = E.t_row[k];
+  if (!have_tcur) E.tcur[k] = E.t_row[k];
+}
+
+// Dependent-chain FMA throughput kernels (8 independent chains per thread).
+template <typename T>
+__global__ void k_fma_peak(T* out, int iters, T seed) {
+  T a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = seed + (T)(threadIdx.x + j);
+  const T m = (T)0.9999999, b = (T)1e-7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = fma(a[j], m, b);
+  }
+  T s = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j];
+  if (s == (T)-1.2345) out[threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rapt_abi_version(void) { return RAPT_GPU_ABI_VERSION; }
+
+void rapt_config_default(rapt_config* g) {
+  std::memset(g, 0, sizeof(*g));
+  g->rtol = 1.49012e-8;  // rapt/__init__.py:21-34
+  g->atol = 1.49012e-8;
+  g->cyclotronresolution = 10;
+  g->gctimestep = 0;
+  g->epss = 5e-2;
+  g->epst = 5e-2;
+  g->nsteps = 500;
+  g->rkf_tol = 1e-3;
+  g->rkf_hmin = 1e-12;
+}
+
+int rapt_ctx_create(int device, void** out) {
+  if (!out) return RAPT_ERR_INVALID;
+  *out = nullptr;
+  Ctx* c = new Ctx();
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) { delete c; return RAPT_ERR_CUDA; }
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->scratch, sizeof(Scratch)) != cudaSuccess ||
+      cudaMallocHost(&c->h_pending, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    delete c;
+    return RAPT_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  register_model_0(&c->tab[0]);
+  register_model_1(&c->tab[1]);
+  register_model_2(&c->tab[2]);
+  register_model_3(&c->tab[3]);
+  register_model_4(&c->tab[4]);
+  register_model_5(&c->tab[5]);
+  register_model_6(&c->tab[6]);
+  register_model_7(&c->tab[7]);
+  rapt_config_default(&c->cfg);
+  *out = c;
+  return RAPT_OK;
+}
+
+void rapt_ctx_destroy(void* ctx) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaFree(c->block);
+  cudaFree(c->scratch);
+  cudaFree(c->tmp);
+  cudaFreeHost(c->h_pending);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* rapt_last_error(const void* ctx) {
+  const Ctx* c = static_cast<const Ctx*>(ctx);
+  return c ? c->err.c_str() : "null context";
+}
+
+int rapt_field_set(void* ctx, int model, const double* params, int nparams) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c) return RAPT_ERR_INVALID;
+  if (model < 0 || model >= RAPT_N_MODELS)
+    return fail(c, RAPT_ERR_UNSUPPORTED, "field model %d has no device implementation", model);
+  if (nparams < 0 || nparams > 8 || (nparams > 0 && !params)) return fail(c, RAPT_ERR_INVALID, "bad field params");
+  build_field(model, params, nparams, &c->field);
+  if (model == RAPT_DOUBLE_DIPOLE && !(c->field.p[2] >= 1))
+    return fail(c, RAPT_ERR_INVALID, "DoubleDipole imagestrength must be >= 1 (fields.py:340)");
+  finish_field(&c->field);
+  c->field_set = true;
+  return RAPT_OK;
+}
+
+int rapt_field_set_steps(void* ctx, double gradientstepsize, double timederivstepsize) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c) return RAPT_ERR_INVALID;
+  if (!c->field_set) return fail(c, RAPT_ERR_STATE, "no field set");
+  if (!(gradientstepsize > 0) || !(timederivstepsize > 0)) return fail(c, RAPT_ERR_INVALID, "step sizes must be > 0");
+  c->field.gradstep = gradientstepsize;
+  c->field.timestep = timederivstepsize;
+  finish_field(&c->field);
+  return RAPT_OK;
+}
+
+int rapt_config_set(void* ctx, const rapt_config* g) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || !g) return RAPT_ERR_INVALID;
+  if (!(g->rtol >= 0) || !(g->atol >= 0) || g->nsteps <= 0 || !(g->cyclotronresolution > 0))
+    return fail(c, RAPT_ERR_INVALID, "bad tolerances, nsteps or cyclotronresolution");
+  if (g->tableau < 0 || g->tableau > 1) return fail(c, RAPT_ERR_INVALID, "tableau must be 0 or 1");
+  if (g->gc_eom < 0 || g->gc_eom > 2) return fail(c, RAPT_ERR_INVALID, "gc_eom must be 0, 1 or 2");
+  if (g->form != RAPT_FORM_PLAIN) return fail(c, RAPT_ERR_UNSUPPORTED, "form %d not available", g->form);
+  c->cfg = *g;
+  return RAPT_OK;
+}
+
+int rapt_ensemble_alloc(void* ctx, int64_t n, int32_t max_rows, int32_t max_switch) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c) return RAPT_ERR_INVALID;
+  if (n <= 0 || max_rows < 2 || max_switch < 0) return fail(c, RAPT_ERR_INVALID, "bad ensemble size");
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  cudaFree(c->block);
+  c->block = nullptr;
+  c->n = 0;
+  const size_t bytes = ensemble_bytes(n, max_rows, max_switch);
+  if (cudaMalloc(&c->block, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, RAPT_ERR_NOMEM, "cudaMalloc(%zu bytes) failed", bytes);
+  }
+  CK(cudaMemsetAsync(c->block, 0, bytes, c->stream));
+  char* p = static_cast<char*>(c->block);
+  DevEnsemble& E = c->E;
+  const size_t N = (size_t)n;
+  E.n = n;
+  E.mode = carve<int8_t>(p, N);
+  E.seg_active = carve<int8_t>(p, N);
+  E.row_mode = carve<int8_t>(p, N * max_rows);
+  E.sw_mode = carve<int8_t>(p, N * max_switch);
+  E.status = carve<int32_t>(p, N);
+  E.flags = carve<int32_t>(p, N);
+  E.nrows = carve<int32_t>(p, N);
+  E.nswitch = carve<int32_t>(p, N);
+  E.nseg = carve<int32_t>(p, N);
+  E.t_int = carve<double>(p, N);
+  E.t_row = carve<double>(p, N);
+  E.tcur = carve<double>(p, N);
+  for (int i = 0; i < 6; ++i) E.s[i] = carve<double>(p, N);
+  E.mu = carve<double>(p, N);
+  E.v = carve<double>(p, N);
+  E.mass = carve<double>(p, N);
+  E.charge = carve<double>(p, N);
+  E.delta = carve<double>(p, N);
+  E.seg_stop = carve<double>(p, N);
+  E.seg_dt = carve<double>(p, N);
+  E.seg_gm = carve<double>(p, N);
+  E.rows = carve<double>(p, N * max_rows * 7);
+  E.sw_time = carve<double>(p, N * max_switch);
+  E.naccept = carve<int64_t>(p, N);
+  E.nreject = carve<int64_t>(p, N);
+  E.nfcn = carve<int64_t>(p, N);
+  c->n = n;
+  c->max_rows = max_rows;
+  c->max_sw = max_switch;
+  CK(cudaStreamSynchronize(c->stream));
+  return RAPT_OK;
+}
+
+int rapt_ensemble_upload(void* ctx, const rapt_host_state* h) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || !h) return RAPT_ERR_INVALID;
+  if (c->n == 0) return fail(c, RAPT_ERR_STATE, "no ensemble allocated");
+  if (h->n != c->n) return fail(c, RAPT_ERR_INVALID, "n %lld != allocated %lld", (long long)h->n, (long long)c->n);
+  if (!h->mode || !h->t_row || !h->s[0] || !h->s[1] || !h->s[2] || !h->s[3] || !h->mass || !h->charge)
+    return fail(c, RAPT_ERR_INVALID, "mode, t_row, s[0..3], mass and charge are required");
+  CK(cudaSetDevice(c->device));
+  const size_t N = (size_t)c->n;
+  DevEnsemble& E = c->E;
+  cudaStream_t s = c->stream;
+  auto up = [&](void* d, const void* hp, size_t bytes) -> cudaError_t {
+    if (hp) return cudaMemcpyAsync(d, hp, bytes, cudaMemcpyHostToDevice, s);
+    return cudaMemsetAsync(d, 0, bytes, s);
+  };
+  CK(up(E.mode, h->mode, N));
+  CK(up(E.status, h->status, N * 4));
+  CK(up(E.flags, h->flags, N * 4));
+  CK(up(E.t_row, h->t_row, N * 8));
+  CK(up(E.t_int, h->t_int, N * 8));
+  CK(up(E.tcur, h->tcur, N * 8));
+  for (int i = 0; i < 6; ++i) CK(up(E.s[i], h->s[i], N * 8));
+  CK(up(E.mu, h->mu, N * 8));
+  CK(up(E.v, h->v, N * 8));
+  CK(up(E.mass, h->mass, N * 8));
+  CK(up(E.charge, h->charge, N * 8));
+  CK(up(E.naccept, h->naccept, N * 8));
+  CK(up(E.nreject, h->nreject, N * 8));
+  CK(up(E.nfcn, h->nfcn, N * 8));
+  CK(up(E.nswitch, h->nswitch, N * 4));
+  CK(cudaMemsetAsync(E.nrows, 0, N * 4, s));
+  k_fill_defaults<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(E, h->t_int != nullptr, h->tcur != nullptr);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s));
+  return RAPT_OK;
+}
+
+int rapt_ensemble_download(void* ctx, rapt_host_state* h) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || !h) return RAPT_ERR_INVALID;
+  if (c->n == 0) return fail(c, RAPT_ERR_STATE, "no ensemble allocated");
+  if (h->n != c->n) return fail(c, RAPT_ERR_INVALID, "n mismatch");
+  CK(cudaSetDevice(c->device));
+  const size_t N = (size_t)c->n;
+  DevEnsemble& E = c->E;
+  cudaStream_t s = c->stream;
+  auto dn = [&](void* hp, const void* d, size_t bytes) -> cudaError_t {
+    return hp ? cudaMemcpyAsync(hp, d, bytes, cudaMemcpyDeviceToHost, s) : cudaSuccess;
+  };
+  CK(dn(h->mode, E.mode, N));
+  CK(dn(h->status, E.status, N * 4));
+  CK(dn(h->flags, E.flags, N * 4));
+  CK(dn(h->t_int, E.t_int, N * 8));
+  CK(dn(h->t_row, E.t_row, N * 8));
+  CK(dn(h->tcur, E.tcur, N * 8));
+  for (int i = 0; i < 6; ++i) CK(dn(h->s[i], E.s[i], N * 8));
+  CK(dn(h->mu, E.mu, N * 8));
+  CK(dn(h->v, E.v, N * 8));
+  CK(dn(h->mass, E.mass, N * 8));
+  CK(dn(h->charge, E.charge, N * 8));
+  CK(dn(h->naccept, E.naccept, N * 8));
+  CK(dn(h->nreject, E.nreject, N * 8));
+  CK(dn(h->nfcn, E.nfcn, N * 8));
+  CK(dn(h->nswitch, E.nswitch, N * 4));
+  CK(cudaStreamSynchronize(s));
+  return RAPT_OK;
+}
+
+int rapt_rows_download(void* ctx, double* rows, int8_t* row_mode, int32_t* nrows, double* sw_time, int8_t* sw_mode,
+                       int reset) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c) return RAPT_ERR_INVALID;
+  if (c->n == 0) return fail(c, RAPT_ERR_STATE, "no ensemble allocated");
+  CK(cudaSetDevice(c->device));
+  const size_t N = (size_t)c->n;
+  DevEnsemble& E = c->E;
+  cudaStream_t s = c->stream;
+  if (rows) CK(cudaMemcpyAsync(rows, E.rows, N * c->max_rows * 7 * 8, cudaMemcpyDeviceToHost, s));
+  if (row_mode) CK(cudaMemcpyAsync(row_mode, E.row_mode, N * c->max_rows, cudaMemcpyDeviceToHost, s));
+  if (nrows) CK(cudaMemcpyAsync(nrows, E.nrows, N * 4, cudaMemcpyDeviceToHost, s));
+  if (sw_time && c->max_sw) CK(cudaMemcpyAsync(sw_time, E.sw_time, N * c->max_sw * 8, cudaMemcpyDeviceToHost, s));
+  if (sw_mode && c->max_sw) CK(cudaMemcpyAsync(sw_mode, E.sw_mode, N * c->max_sw, cudaMemcpyDeviceToHost, s));
+  if (reset) {
+    CK(cudaMemsetAsync(E.nrows, 0, N * 4, s));
+    CK(cudaMemsetAsync(E.nswitch, 0, N * 4, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  return RAPT_OK;
+}
+
+int rapt_advance(void* ctx, int kind, const double* delta, double delta_all, rapt_stats* stats) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c) return RAPT_ERR_INVALID;
+  if (!c->field_set) return fail(c, RAPT_ERR_STATE, "no field set");
+  if (c->n == 0) return fail(c, RAPT_ERR_STATE, "no ensemble allocated");
+  if (kind < RAPT_KIND_PARTICLE || kind > RAPT_KIND_ADAPTIVE) return fail(c, RAPT_ERR_INVALID, "bad kind");
+  if (!delta && !std::isfinite(delta_all)) return fail(c, RAPT_ERR_INVALID, "delta must be finite");
+  CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  DevEnsemble& E = c->E;
+  const size_t N = (size_t)c->n;
+  double* d_delta = nullptr;
+  if (delta) {
+    if (c->tmp_bytes < N * 8) {
+      cudaFree(c->tmp);
+      c->tmp = nullptr;
+      c->tmp_bytes = 0;
+      CK(cudaMalloc(&c->tmp, N * 8));
+      c->tmp_bytes = N * 8;
+    }
+    d_delta = static_cast<double*>(c->tmp);
+    CK(cudaMemcpyAsync(d_delta, delta, N * 8, cudaMemcpyHostToDevice, s));
+  }
+  const KParams P = make_params(c, kind);
+  const ModelTable& T = c->tab[c->field.model];
+  const int tab = c->cfg.tableau;
+  const int block = c->cfg.threads_per_block > 0 ? c->cfg.threads_per_block : 128;
+  if (block % 32 != 0 || block > 128) return fail(c, RAPT_ERR_INVALID, "threads_per_block must be a multiple of 32, <= 128");
+  int bps_p = T.occ_particle[tab](block), bps_g = T.occ_gc[tab](block);
+  if (c->cfg.blocks_per_sm > 0) {
+    bps_p = std::min(bps_p, c->cfg.blocks_per_sm);
+    bps_g = std::min(bps_g, c->cfg.blocks_per_sm);
+  }
+  if (bps_p < 1 || bps_g < 1) return fail(c, RAPT_ERR_CUDA, "kernel does not fit on an SM");
+
+  CK(cudaEventRecord(c->ev0, s));
+  k_prepare<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(E, d_delta, delta_all, kind);
+  CK(cudaGetLastError());
+  CK(cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), s));
+  int64_t launches = 0, kl = 1;
+  const int max_rounds = 1000000;
+  int round = 0;
+  for (; round < max_rounds; ++round) {
+    CK(cudaMemsetAsync(c->scratch, 0, 3 * sizeof(unsigned long long), s));  // queue[2], pending
+    LaunchArgs a{E, P, c->scratch, 0, block, s};
+    if (kind != RAPT_KIND_GC) {
+      a.grid = c->num_sms * bps_p;
+      CK(T.particle[tab](a));
+      ++kl;
+    }
+    if (kind != RAPT_KIND_PARTICLE) {
+      a.grid = c->num_sms * bps_g;
+      CK(T.gc[tab](a));
+      ++kl;
+    }
+    ++launches;
+    CK(cudaMemcpyAsync(c->h_pending, &c->scratch->pending, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (*c->h_pending == 0) break;
+  }
+  CK(cudaEventRecord(c->ev1, s));
+  Scratch hs;
+  CK(cudaMemcpyAsync(&hs, c->scratch, sizeof(Scratch), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (stats) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    stats->accepted = (int64_t)hs.accepted;
+    stats->rejected = (int64_t)hs.rejected;
+    stats->rhs_evals = (int64_t)hs.rhs;
+    stats->switches = (int64_t)hs.switches;
+    stats->done = (int64_t)hs.done;
+    stats->failed = (int64_t)hs.failed;
+    stats->launches = launches;
+    stats->kernel_launches = kl;
+    stats->kernel_ms = ms;
+  }
+  if (round >= max_rounds) return fail(c, RAPT_ERR_STATE, "advance did not finish in %d rounds", max_rounds);
+  return RAPT_OK;
+}
+
+int rapt_adaptive_init(void* ctx) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c) return RAPT_ERR_INVALID;
+  if (!c->field_set || c->n == 0) return fail(c, RAPT_ERR_STATE, "field and ensemble required");
+  CK(cudaSetDevice(c->device));
+  const KParams P = make_params(c, RAPT_KIND_ADAPTIVE);
+  CK(c->tab[c->field.model].adaptive_init(c->E, P, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return RAPT_OK;
+}
+
+static int ensure_tmp(Ctx* c, size_t bytes) {
+  if (c->tmp_bytes >= bytes) return RAPT_OK;
+  cudaFree(c->tmp);
+  c->tmp = nullptr;
+  c->tmp_bytes = 0;
+  CK(cudaMalloc(&c->tmp, bytes));
+  c->tmp_bytes = bytes;
+  return RAPT_OK;
+}
+
+int rapt_field_eval(void* ctx, int what, int64_t n, const double* tpos, double* out) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || n < 0 || (n > 0 && (!tpos || !out))) return RAPT_ERR_INVALID;
+  if (!c->field_set) return fail(c, RAPT_ERR_STATE, "no field set");
+  if (what < 0 || what > 10) return fail(c, RAPT_ERR_INVALID, "bad quantity %d", what);
+  if (n == 0) return RAPT_OK;
+  CK(cudaSetDevice(c->device));
+  const size_t N = (size_t)n;
+  int rc = ensure_tmp(c, N * 13 * 8);
+  if (rc) return rc;
+  double* d_in = static_cast<double*>(c->tmp);
+  double* d_out = d_in + 4 * N;
+  CK(cudaMemcpyAsync(d_in, tpos, N * 32, cudaMemcpyHostToDevice, c->stream));
+  CK(c->tab[c->field.model].field_eval(c->field, what, n, d_in, d_out, c->stream));
+  CK(cudaMemcpyAsync(out, d_out, N * 72, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return RAPT_OK;
+}
+
+int rapt_rhs_eval(void* ctx, int mode, int64_t n, const double* state, const double* mass, const double* charge,
+                  const double* v, double* out) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || n < 0 || (n > 0 && (!state || !mass || !charge || !out))) return RAPT_ERR_INVALID;
+  if (!c->field_set) return fail(c, RAPT_ERR_STATE, "no field set");
+  if (mode == RAPT_MODE_GC && !v) return fail(c, RAPT_ERR_INVALID, "GC needs v");
+  if (n == 0) return RAPT_OK;
+  CK(cudaSetDevice(c->device));
+  const size_t N = (size_t)n;
+  int rc = ensure_tmp(c, N * 17 * 8);
+  if (rc) return rc;
+  double* d = static_cast<double*>(c->tmp);
+  double *d_state = d, *d_mass = d + 8 * N, *d_charge = d + 9 * N, *d_v = d + 10 * N, *d_out = d + 11 * N;
+  CK(cudaMemcpyAsync(d_state, state, N * 64, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(d_mass, mass, N * 8, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(d_charge, charge, N * 8, cudaMemcpyHostToDevice, c->stream));
+  if (v) CK(cudaMemcpyAsync(d_v, v, N * 8, cudaMemcpyHostToDevice, c->stream));
+  else CK(cudaMemsetAsync(d_v, 0, N * 8, c->stream));
+  const KParams P = make_params(c, RAPT_KIND_PARTICLE);
+  CK(c->tab[c->field.model].rhs_eval(P, mode, n, d_state, d_mass, d_charge, d_v, d_out, c->stream));
+  CK(cudaMemcpyAsync(out, d_out, N * 48, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return RAPT_OK;
+}
+
+int rapt_host_register(void* p, uint64_t bytes) {
+  if (!p || bytes == 0) return RAPT_ERR_INVALID;
+  return cudaHostRegister(p, (size_t)bytes, cudaHostRegisterDefault) == cudaSuccess ? RAPT_OK : RAPT_ERR_CUDA;
+}
+
+int rapt_host_unregister(void* p) {
+  if (!p) return RAPT_ERR_INVALID;
+  return cudaHostUnregister(p) == cudaSuccess ? RAPT_OK : RAPT_ERR_CUDA;
+}
+
+int rapt_measure_peaks(void* ctx, double* fp64_tflops, double* fp32_tflops) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c) return RAPT_ERR_INVALID;
+  CK(cudaSetDevice(c->device));
+  int rc = ensure_tmp(c, 4096 * 8);
+  if (rc) return rc;
+  const int blocks = c->num_sms * 4, threads = 256;
+  auto run = [&](auto tag, int iters, double* out_tflops) -> int {
+    using T = decltype(tag);
+    for (int rep = 0; rep < 2; ++rep) {
+      CK(cudaEventRecord(c->ev0, c->stream));
+      k_fma_peak<T><<<blocks, threads, 0, c->stream>>>(static_cast<T*>(c->tmp), iters, (T)1.0);
+      CK(cudaGetLastError());
+      CK(cudaEventRecord(c->ev1, c->stream));
+      CK(cudaEventSynchronize(c->ev1));
+    }
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
+    *out_tflops = flops / (ms * 1e-3) / 1e12;
+    return RAPT_OK;
+  };
+  double a = 0, b = 0;
+  rc = run(double(0), 4096, &a);
+  if (rc) return rc;
+  rc = run(float(0), 65536, &b);
+  if (rc) return rc;
+  if (fp64_tflops) *fp64_tflops = a;
+  if (fp32_tflops) *fp32_tflops = b;
+  return RAPT_OK;
+}
+
+}  // extern "C"

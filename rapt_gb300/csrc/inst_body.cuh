@@ -1,0 +1,66 @@
+// inst_body.cuh -- instantiates every kernel for one field model. Included by
+// inst_model<k>.cu with RAPT_MODEL defined, so the models compile in parallel.
+#include "eval_kernels.cuh"
+#include "launch.h"
+
+#define RAPT_CAT2(a, b) a##b
+#define RAPT_CAT(a, b) RAPT_CAT2(a, b)
+
+namespace rapt {
+namespace {
+constexpr int kM = RAPT_MODEL;
+
+template <int TAB>
+cudaError_t launch_particle(const LaunchArgs& a) {
+  k_particle<kM, TAB><<<a.grid, a.block, 0, a.stream>>>(a.E, a.P, a.S);
+  return cudaGetLastError();
+}
+template <int TAB>
+cudaError_t launch_gc(const LaunchArgs& a) {
+  k_gc<kM, TAB><<<a.grid, a.block, 0, a.stream>>>(a.E, a.P, a.S);
+  return cudaGetLastError();
+}
+template <int TAB>
+int occ_particle(int block) {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_particle<kM, TAB>, block, 0);
+  return nb;
+}
+template <int TAB>
+int occ_gc(int block) {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc<kM, TAB>, block, 0);
+  return nb;
+}
+cudaError_t field_eval(const FieldP& f, int what, int64_t n, const double* tpos, double* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_field_eval<kM><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(f, what, n, tpos, out);
+  return cudaGetLastError();
+}
+cudaError_t rhs_eval(const KParams& P, int mode, int64_t n, const double* state, const double* mass,
+                     const double* charge, const double* v, double* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_rhs_eval<kM><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(P, mode, n, state, mass, charge, v, out);
+  return cudaGetLastError();
+}
+cudaError_t adaptive_init(const DevEnsemble& E, const KParams& P, cudaStream_t s) {
+  if (E.n <= 0) return cudaSuccess;
+  k_adaptive_init<kM><<<(unsigned)((E.n + 127) / 128), 128, 0, s>>>(E, P);
+  return cudaGetLastError();
+}
+}  // namespace
+
+void RAPT_CAT(register_model_, RAPT_MODEL)(ModelTable* t) {
+  t->particle[0] = launch_particle<0>;
+  t->particle[1] = launch_particle<1>;
+  t->gc[0] = launch_gc<0>;
+  t->gc[1] = launch_gc<1>;
+  t->occ_particle[0] = occ_particle<0>;
+  t->occ_particle[1] = occ_particle<1>;
+  t->occ_gc[0] = occ_gc<0>;
+  t->occ_gc[1] = occ_gc<1>;
+  t->field_eval = field_eval;
+  t->rhs_eval = rhs_eval;
+  t->adaptive_init = adaptive_init;
+}
+}  // namespace rapt

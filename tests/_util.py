@@ -1,0 +1,71 @@
+"""Shared helpers of the test suite: build the same tracers for the GPU ensemble
+and for the CPU oracle, and compare them."""
+import numpy as np
+
+from rapt_gb300 import fields as F
+
+
+def field_of(w):
+    name, kw = w["field"]
+    return getattr(F, name)(**kw)
+
+
+def oracle_field(O, w):
+    name, kw = w["field"]
+    fld = field_of(w)
+    return O.field(name, fld.device_params())
+
+
+def oracle_config(O, w, **over):
+    p = dict(w["params"])
+    p.update(over)
+    return O.config(rtol=p.get("rtol", 1.49012e-8), atol=p.get("atol", 1.49012e-8),
+                    cycres=p.get("cyclotronresolution", 10), gctimestep=p.get("gctimestep", 0.0),
+                    epss=p.get("epss", 5e-2), epst=p.get("epst", 5e-2), tableau=p.get("tableau", 0),
+                    gc_eom=p.get("gc_eom", 0), nsteps=p.get("nsteps", 500),
+                    rkf_tol=p.get("rkf_tol", 1e-3), rkf_hmin=p.get("rkf_hmin", 1e-12),
+                    enforce_equatorial=p.get("enforce_equatorial", 0))
+
+
+def oracle_tracers(O, w, kind):
+    n = len(w["mass"])
+    f = oracle_field(O, w)
+    cfg = oracle_config(O, w)
+    out = []
+    for i in range(n):
+        if kind == "gc":
+            out.append(O.gc_new_pa(f, w["pos"][i], w["v"][i], w["pa"][i], 0.0, w["mass"][i], w["charge"][i]))
+        elif kind == "particle":
+            out.append(O.particle_new(w["pos"][i], w["vel"][i], 0.0, w["mass"][i], w["charge"][i]))
+        else:
+            out.append(O.adaptive_init(f, cfg, w["pos"][i], w["vel"][i], 0.0, w["mass"][i], w["charge"][i]))
+    return f, cfg, O.tracers_from_structs(out)
+
+
+def gpu_ensemble(w, kind, max_rows=4, max_switch=0, **over):
+    from rapt_gb300 import Ensemble
+    n = len(w["mass"])
+    ens = Ensemble(field_of(w), n, max_rows=max_rows, max_switch=max_switch)
+    p = dict(w["params"])
+    p.update(over)
+    ens.configure(**p)
+    if kind == "gc":
+        ens.set_guiding_centers(w["pos"], w["v"], pa=w["pa"], t0=0.0, mass=w["mass"], charge=w["charge"])
+    else:
+        ens.set_particles(w["pos"], w["vel"], 0.0, w["mass"], w["charge"])
+    ens.upload()
+    if kind == "adaptive":
+        ens.adaptive_init()
+    return ens
+
+
+def rel_state_error(gpu_s, orc_s, ncomp):
+    """Per-tracer relative error of position and of momentum (or ppar)."""
+    g = np.asarray(gpu_s)[:ncomp].T
+    o = np.asarray(orc_s)[:, :ncomp]
+    pos = np.linalg.norm(g[:, :3] - o[:, :3], axis=1) / np.linalg.norm(o[:, :3], axis=1)
+    if ncomp == 6:
+        mom = np.linalg.norm(g[:, 3:6] - o[:, 3:6], axis=1) / np.linalg.norm(o[:, 3:6], axis=1)
+    else:
+        mom = np.abs(g[:, 3] - o[:, 3]) / np.maximum(np.abs(o[:, 3]), 1e-300)
+    return pos, mom
