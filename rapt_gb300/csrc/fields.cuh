@@ -4,6 +4,12 @@
 // instantiated per model with no runtime dispatch in the right-hand side.
 // Powers of r use one FP64 rsqrt instead of the reference's pow(r2, 2.5) and
 // division (same quantity, different rounding: a few ulp).
+//
+// Values that feed a central difference (field components, |B|, unit vectors)
+// end in an explicitly rounded multiply (__dmul_rn): otherwise the compiler may
+// fuse the last product into the difference, which then sees the unrounded
+// product and no longer takes the difference of two field values as the
+// reference's scheme does (a constant field would get a nonzero gradient).
 #pragma once
 #include "common.cuh"
 
@@ -22,9 +28,9 @@ struct Field<RAPT_EARTH_DIPOLE> {
     const double ri = rsqrt(r2);
     const double ri2 = ri * ri;
     const double s = f.c0 * (ri2 * ri2 * ri);
-    o[0] = s * (x * z);
-    o[1] = s * (y * z);
-    o[2] = s * (z * z - r2 * (1.0 / 3.0));
+    o[0] = __dmul_rn(s, x * z);
+    o[1] = __dmul_rn(s, y * z);
+    o[2] = __dmul_rn(s, z * z - r2 * (1.0 / 3.0));
   }
   __device__ __forceinline__ static void E(const FieldP&, double, double, double, double, double* o) {
     o[0] = o[1] = o[2] = 0.0;
@@ -49,9 +55,9 @@ struct Field<RAPT_DOUBLE_DIPOLE> {
     const double sb = f.p[2] * (ib2 * ib2 * ib);
     const double tz = 3.0 * z;
     const double zz2 = 2.0 * z * z;
-    o[0] = f.c0 * (tz * (x * sa + x2 * sb));
-    o[1] = f.c0 * (tz * y * (sa + sb));
-    o[2] = f.c0 * ((zz2 - x * x - y * y) * sa + (zz2 - x2 * x2 - y * y) * sb);
+    o[0] = __dmul_rn(f.c0, tz * (x * sa + x2 * sb));
+    o[1] = __dmul_rn(f.c0, tz * y * (sa + sb));
+    o[2] = __dmul_rn(f.c0, (zz2 - x * x - y * y) * sa + (zz2 - x2 * x2 - y * y) * sb);
   }
   __device__ __forceinline__ static void E(const FieldP&, double, double, double, double, double* o) {
     o[0] = o[1] = o[2] = 0.0;
@@ -92,9 +98,9 @@ struct Field<RAPT_VAR_EARTH_DIPOLE> {
     const double ri = rsqrt(r2);
     const double ri2 = ri * ri;
     const double s = f.c0 * (1.0 + f.p[0] * sin(f.c1 * t)) * (ri2 * ri2 * ri);
-    o[0] = s * (3.0 * x * z);
-    o[1] = s * (3.0 * y * z);
-    o[2] = s * (2.0 * z * z - x * x - y * y);
+    o[0] = __dmul_rn(s, 3.0 * x * z);
+    o[1] = __dmul_rn(s, 3.0 * y * z);
+    o[2] = __dmul_rn(s, 2.0 * z * z - x * x - y * y);
   }
   __device__ __forceinline__ static void E(const FieldP&, double, double, double, double, double* o) {
     o[0] = o[1] = o[2] = 0.0;
@@ -123,7 +129,7 @@ template <>
 struct Field<RAPT_HARRIS> {
   static constexpr bool kStatic = false;
   __device__ __forceinline__ static void B(const FieldP& f, double, double, double, double z, double* o) {
-    o[0] = f.p[0] * tanh(z * f.c0);
+    o[0] = __dmul_rn(f.p[0], tanh(z * f.c0));
     o[1] = 0.0;
     o[2] = f.p[2];
   }
@@ -143,9 +149,9 @@ struct Field<RAPT_COMPRESSED_DIPOLE> {
     const double ri = rsqrt(r2);
     const double ri2 = ri * ri;
     const double s = f.c0 * (1.0 + f.p[1] * sin(f.c1 * t)) * (ri2 * ri2 * ri);
-    o[0] = s * (3.0 * x * z);
-    o[1] = s * (3.0 * y * z);
-    o[2] = s * (2.0 * z * z - x * x - y * y);
+    o[0] = __dmul_rn(s, 3.0 * x * z);
+    o[1] = __dmul_rn(s, 3.0 * y * z);
+    o[2] = __dmul_rn(s, 2.0 * z * z - x * x - y * y);
   }
   __device__ __forceinline__ static void E(const FieldP& f, double t, double x, double y, double z, double* o) {
     const double r2 = x * x + y * y + z * z;
@@ -165,8 +171,8 @@ __device__ __forceinline__ void unit_and_mag(const FieldP& f, double t, double x
   Field<M>::B(f, t, x, y, z, b);
   const double b2 = dot3(b, b);
   const double ib = rsqrt(b2);
-  mag = b2 * ib;
-  ub[0] = b[0] * ib; ub[1] = b[1] * ib; ub[2] = b[2] * ib;
+  mag = __dmul_rn(b2, ib);
+  ub[0] = __dmul_rn(b[0], ib); ub[1] = __dmul_rn(b[1], ib); ub[2] = __dmul_rn(b[2], ib);
 }
 
 // The reference's central-difference stencil (fields.py:111-131 gradB and

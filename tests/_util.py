@@ -69,3 +69,25 @@ def rel_state_error(gpu_s, orc_s, ncomp):
     else:
         mom = np.abs(g[:, 3] - o[:, 3]) / np.maximum(np.abs(o[:, 3]), 1e-300)
     return pos, mom
+
+
+def sensitivity_envelope(O, w, kind, delta, rel=1e-15, **over):
+    """Per-tracer divergence of the oracle from itself when the start position and
+    momentum are scaled by (1 + rel): how far rounding-level differences can grow
+    along each trajectory (large for chaotic, nonadiabatic orbits)."""
+    w2 = dict(w)
+    if kind == "gc":
+        w2["pos"] = w["pos"] * (1 + rel)
+    else:
+        w2["pos"] = w["pos"] * (1 + rel)
+        w2["vel"] = w["vel"] * (1 + rel)
+    f, cfg, a = oracle_tracers(O, w, kind)
+    _, _, b = oracle_tracers(O, w2, kind)
+    if over:
+        cfg = oracle_config(O, w, **over)
+    k = {"particle": 0, "gc": 1, "adaptive": 2}[kind]
+    O.batch_advance(f, cfg, k, a, delta)
+    O.batch_advance(f, cfg, k, b, delta)
+    n = 6 if kind == "particle" else 4
+    pos, mom = rel_state_error(a["s"].T, b["s"], n)
+    return a, pos, mom
