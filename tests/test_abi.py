@@ -1,0 +1,52 @@
+"""CPU checks of the C ABI boundary: the library loads without a GPU, exports
+every function include/rapt_gpu.h declares, and its ctypes layouts match the
+header's structs. No compute call is made."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from rapt_gb300 import _native as N
+
+HDR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "rapt_gpu.h")
+
+
+def _declared():
+    src = open(HDR).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(rapt_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = N.lib()
+    names = _declared()
+    assert len(names) >= 20
+    for name in names:
+        assert hasattr(L, name), name
+    assert set(names) == set(N.SIGNATURES), set(names) ^ set(N.SIGNATURES)
+
+
+def test_abi_version_and_defaults():
+    L = N.lib()
+    assert L.rapt_abi_version() == 1
+    cfg = N.RaptConfig()
+    L.rapt_config_default(C.byref(cfg))
+    assert cfg.rtol == cfg.atol == 1.49012e-8   # rapt/__init__.py:27
+    assert cfg.cyclotronresolution == 10 and cfg.nsteps == 500 and cfg.epss == cfg.epst == 0.05
+
+
+def test_struct_layouts_match_header():
+    # field order and sizes of rapt_config / rapt_host_state / rapt_stats / rapt_gc_device_state
+    assert C.sizeof(N.RaptConfig) == 8 * 6 + 4 * 4 + 8 * 2 + 4 * 2 + 8 + 4 * 2
+    assert C.sizeof(N.RaptHostState) == 8 * 21
+    assert C.sizeof(N.RaptStats) == 8 * 9
+    assert C.sizeof(N.RaptGcDeviceState) == 8 * 18
+
+
+def test_no_gpu_fails_loudly_without_fallback():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(N.RaptError):
+        N.Context(0)
