@@ -181,6 +181,50 @@ int rapt_field_eval(void* ctx, int what, int64_t n, const double* tpos, double* 
 int rapt_rhs_eval(void* ctx, int mode, int64_t n, const double* state, const double* mass,
                   const double* charge, const double* v, double* out);
 
+/* --- allocation-free guiding-centre advance ------------------------------- */
+/* No counterpart in the reference: RAPT has no device code and no notion of
+ * memory ownership. This entry point is for callers that cannot call
+ * cudaMalloc -- applications that must not allocate once running (real-time
+ * loops), libraries that own all device memory through their own pool, and code
+ * that must not trigger the implicit device synchronisation an allocation or
+ * free can cause. It advances up to RAPT_NOALLOC_MAX_TRACERS guiding centres
+ * (GuidingCenter.advance, GuidingCenter.py:397-458, kind RAPT_KIND_GC) whose
+ * state lives in caller-owned device memory, creates no context, and allocates
+ * nothing: the work-queue heads, counters and per-tracer bookkeeping live in one
+ * fixed __device__ array of RAPT_NOALLOC_SCRATCH_BYTES that every GPU loading
+ * the library holds until the process exits.
+ *  - n > RAPT_NOALLOC_MAX_TRACERS returns RAPT_ERR_INVALID and touches nothing.
+ *  - The first call on a device looks up that array's address; make it before
+ *    any stream capture on that device.
+ *  - All calls share the array: calls whose GPU work overlaps (other threads or
+ *    streams on the same device) race and must be serialised by the caller.
+ *  - nrows is reset to 0 by each call; rows[n][max_rows][7] receive the rows
+ *    (t, x, y, z, ppar, 0, 0) of this call. Returns after the work completes. */
+#define RAPT_NOALLOC_MAX_TRACERS 65536
+#define RAPT_NOALLOC_SCRATCH_BYTES 5242880
+typedef struct {
+  int64_t n;
+  double* t;              /* in/out: time of the last trajectory row */
+  double* x;              /* in/out */
+  double* y;              /* in/out */
+  double* z;              /* in/out */
+  double* ppar;           /* in/out: parallel momentum */
+  const double* mu;       /* in */
+  const double* v;        /* in: GuidingCenter.v */
+  const double* mass;     /* in */
+  const double* charge;   /* in */
+  int32_t* status;        /* out: RAPT_ST_* */
+  int64_t* naccept;       /* in/out: accumulated */
+  int64_t* nreject;       /* in/out */
+  int64_t* nfcn;          /* in/out */
+  double* rows;           /* out */
+  int8_t* row_mode;       /* out */
+  int32_t* nrows;         /* out */
+  int32_t max_rows;       /* rows per tracer, >= 2 */
+} rapt_gc_device_state;
+int rapt_gc_advance_noalloc(int device, int model, const double* params, int nparams, const rapt_config* cfg,
+                            const rapt_gc_device_state* state, double delta, void* stream, rapt_stats* stats);
+
 /* Page-lock (pin) a caller-owned host buffer so that uploads and downloads
  * through it run at full PCIe/NVLink-C2C speed; unregister before freeing. */
 int rapt_host_register(void* p, uint64_t bytes);

@@ -75,7 +75,20 @@ SIGNATURES = {
     "rapt_measure_peaks": (C.c_int, [_VP, _DP, _DP]),
     "rapt_host_register": (C.c_int, [_VP, C.c_uint64]),
     "rapt_host_unregister": (C.c_int, [_VP]),
+    "rapt_gc_advance_noalloc": (C.c_int, [C.c_int, C.c_int, _DP, C.c_int, C.POINTER(RaptConfig), _VP, _D, _VP,
+                                          C.POINTER(RaptStats)]),
 }
+
+NOALLOC_MAX_TRACERS = 65536
+
+
+class RaptGcDeviceState(C.Structure):
+    """rapt_gc_device_state: device pointers of a caller-owned guiding-centre ensemble."""
+    _fields_ = [("n", C.c_int64), ("t", C.c_void_p), ("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
+                ("ppar", C.c_void_p), ("mu", C.c_void_p), ("v", C.c_void_p), ("mass", C.c_void_p),
+                ("charge", C.c_void_p), ("status", C.c_void_p), ("naccept", C.c_void_p),
+                ("nreject", C.c_void_p), ("nfcn", C.c_void_p), ("rows", C.c_void_p), ("row_mode", C.c_void_p),
+                ("nrows", C.c_void_p), ("max_rows", C.c_int32)]
 
 _lib = None
 
