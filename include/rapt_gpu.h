@@ -164,6 +164,9 @@ int rapt_rows_download(void* ctx, double* rows, int8_t* row_mode, int32_t* nrows
  * for every tracer of the ensemble at once. delta: per-tracer array (length n)
  * or NULL to use delta_all. Returns when the device work has completed. */
 int rapt_advance(void* ctx, int kind, const double* delta, double delta_all, rapt_stats* stats);
+/* Continue the last rapt_advance after tracers stopped with RAPT_ST_ROWS_FULL
+ * (drain their rows with rapt_rows_download(..., reset=1) first). */
+int rapt_advance_resume(void* ctx, int kind, rapt_stats* stats);
 
 /* Adaptive.__init__ mode pick (Adaptive.py:70-104) on device: tracers given as
  * particles are converted to guiding centres where Particle.isadiabatic() holds. */

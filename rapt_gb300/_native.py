@@ -69,6 +69,7 @@ SIGNATURES = {
     "rapt_ensemble_download": (C.c_int, [_VP, C.POINTER(RaptHostState)]),
     "rapt_rows_download": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int]),
     "rapt_advance": (C.c_int, [_VP, C.c_int, _VP, _D, C.POINTER(RaptStats)]),
+    "rapt_advance_resume": (C.c_int, [_VP, C.c_int, C.POINTER(RaptStats)]),
     "rapt_adaptive_init": (C.c_int, [_VP]),
     "rapt_field_eval": (C.c_int, [_VP, C.c_int, _I64, _VP, _VP]),
     "rapt_rhs_eval": (C.c_int, [_VP, C.c_int, _I64, _VP, _VP, _VP, _VP, _VP]),

@@ -409,13 +409,30 @@ int rapt_rows_download(void* ctx, double* rows, int8_t* row_mode, int32_t* nrows
   return RAPT_OK;
 }
 
+__global__ void k_clear_rows_full(DevEnsemble E) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < E.n && E.status[k] == RAPT_ST_ROWS_FULL) E.status[k] = RAPT_ST_OK;
+}
+
+static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all, rapt_stats* stats, bool resume);
+
 int rapt_advance(void* ctx, int kind, const double* delta, double delta_all, rapt_stats* stats) {
   Ctx* c = static_cast<Ctx*>(ctx);
   if (!c) return RAPT_ERR_INVALID;
+  return advance_impl(c, kind, delta, delta_all, stats, false);
+}
+
+int rapt_advance_resume(void* ctx, int kind, rapt_stats* stats) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c) return RAPT_ERR_INVALID;
+  return advance_impl(c, kind, nullptr, 0.0, stats, true);
+}
+
+static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all, rapt_stats* stats, bool resume) {
   if (!c->field_set) return fail(c, RAPT_ERR_STATE, "no field set");
   if (c->n == 0) return fail(c, RAPT_ERR_STATE, "no ensemble allocated");
   if (kind < RAPT_KIND_PARTICLE || kind > RAPT_KIND_ADAPTIVE) return fail(c, RAPT_ERR_INVALID, "bad kind");
-  if (!delta && !std::isfinite(delta_all)) return fail(c, RAPT_ERR_INVALID, "delta must be finite");
+  if (!resume && !delta && !std::isfinite(delta_all)) return fail(c, RAPT_ERR_INVALID, "delta must be finite");
   CK(cudaSetDevice(c->device));
   cudaStream_t s = c->stream;
   DevEnsemble& E = c->E;
@@ -445,7 +462,8 @@ int rapt_advance(void* ctx, int kind, const double* delta, double delta_all, rap
   if (bps_p < 1 || bps_g < 1) return fail(c, RAPT_ERR_CUDA, "kernel does not fit on an SM");
 
   CK(cudaEventRecord(c->ev0, s));
-  k_prepare<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(E, d_delta, delta_all, kind);
+  if (resume) k_clear_rows_full<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(E);
+  else k_prepare<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(E, d_delta, delta_all, kind);
   CK(cudaGetLastError());
   CK(cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), s));
   int64_t launches = 0, kl = 1;

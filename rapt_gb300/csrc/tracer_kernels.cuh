@@ -484,7 +484,10 @@ __global__ void __launch_bounds__(128) k_particle(DevEnsemble E, KParams P, Scra
             }
             ++nsw;
             nswitch = nsw;
-            put_row(E, P, idx, nrows, t_row, y, 4, RAPT_MODE_GC);
+            // the first row of a guiding-centre segment carries its mu and v in
+            // the two columns a guiding-centre row does not use
+            const double first[6] = {g[0], g[1], g[2], g[3], mu, vs};
+            put_row(E, P, idx, nrows, t_row, first, 6, RAPT_MODE_GC);
             st.sw++;
             st.pend++;
           } else {

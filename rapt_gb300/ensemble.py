@@ -176,3 +176,13 @@ class Ensemble:
         self.ctx.check(rc, "rapt_advance")
         self.last_stats = st.as_dict()
         return self.last_stats
+
+    def advance_resume(self, kind):
+        """Continue the last advance after tracers stopped with a full row buffer
+        (drain it with ``rows(reset=True)`` first)."""
+        kind = {"particle": N.KIND_PARTICLE, "gc": N.KIND_GC, "adaptive": N.KIND_ADAPTIVE}.get(kind, kind)
+        self.field.bind(self.ctx)
+        st = N.RaptStats()
+        self.ctx.check(self.ctx.L.rapt_advance_resume(self.ctx.h, int(kind), N.ctypes_byref(st)), "rapt_advance_resume")
+        self.last_stats = st.as_dict()
+        return self.last_stats

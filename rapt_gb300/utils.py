@@ -1,0 +1,132 @@
+"""Physics utilities of rapt/utils.py used by the tracer classes (host side).
+
+Field quantities are evaluated by the GPU library through the field objects.
+Formulas and evaluation order follow rapt/utils.py (line numbers cited).
+"""
+import numpy as np
+
+c = 299792458
+e = 1.602176565e-19
+
+
+def gamma(mass=0, **kwargs):
+    """rapt/utils.py:15-27."""
+    if "velocity" in kwargs:
+        return 1 / np.sqrt(1 - np.dot(kwargs["velocity"], kwargs["velocity"]) / c ** 2)
+    elif "momentum" in kwargs:
+        if mass == 0:
+            raise ValueError("Particle mass not given.")
+        return np.sqrt(1 + np.dot(kwargs["momentum"], kwargs["momentum"]) / (mass * c) ** 2)
+    raise ValueError("Either velocity of momentum vectors should be given.")
+
+
+def cyclotron_period(t, pos, vel, field, mass, charge):
+    """rapt/utils.py:29-66: 2 pi gamma m / (q B) from the velocity vector."""
+    vel = np.array(vel)
+    g = 1.0 / np.sqrt(1 - np.dot(vel, vel) / c ** 2)
+    B = field.magB(np.concatenate([[t], pos]))
+    return 2 * np.pi * g * mass / B / abs(charge)
+
+
+def cyclotron_period2(t, pos, speed, field, mass, charge):
+    """rapt/utils.py:68-104: from the speed."""
+    g = 1.0 / np.sqrt(1 - (speed / c) ** 2)
+    B = field.magB(np.concatenate([[t], pos]))
+    return 2 * np.pi * g * mass / B / abs(charge)
+
+
+def cyclotron_radius(t, pos, vel, field, mass, charge):
+    """rapt/utils.py:106-145."""
+    vsq = np.dot(vel, vel)
+    g = 1.0 / np.sqrt(1 - vsq / c ** 2)
+    B = field.B(np.concatenate([[t], pos]))
+    Bmag = np.sqrt(np.dot(B, B))
+    vpar = np.dot(vel, B) / Bmag
+    vperp = np.sqrt(vsq - vpar ** 2)
+    return g * mass * vperp / (abs(charge) * Bmag)
+
+
+def cyclotron_radius2(t, pos, vpar, v, field, mass, charge):
+    """rapt/utils.py:147-187."""
+    g = 1.0 / np.sqrt(1 - (v / c) ** 2)
+    B = field.B(np.concatenate([[t], pos]))
+    Bmag = np.sqrt(np.dot(B, B))
+    vperp = np.sqrt((v - vpar) * (v + vpar))
+    return g * mass * vperp / (abs(charge) * Bmag)
+
+
+def magnetic_moment(t, pos, vpar, v, field, mass):
+    """rapt/utils.py:189-216: gamma^2 m v_perp^2 / (2 B)."""
+    g = 1.0 / np.sqrt(1 - (v / c) ** 2)
+    Bmag = field.magB(np.concatenate([[t], pos]))
+    return g ** 2 * mass * (v - vpar) * (v + vpar) / (2 * Bmag)
+
+
+def speedfromKE(KE, mass, unit="ev"):
+    """rapt/utils.py:218-249."""
+    mc2 = mass * c ** 2
+    if unit.lower() == "ev":
+        KE = KE * e
+    if KE / mc2 < 1e-6:
+        return np.sqrt(2 * KE / mass)
+    return c * np.sqrt(1 - (mc2 / (mc2 + KE)) ** 2)
+
+
+def guidingcenter(t, r, v, field, mass, charge, tol=1e-3, maxiter=20, debug=False):
+    """rapt/utils.py:251-326: fixed point R = r - rho(R). Returns None (after a
+    message) when it does not converge, as the reference does."""
+    def gyrovector(rr):
+        vsq = np.dot(v, v)
+        g = 1 / np.sqrt(1 - vsq / c ** 2)
+        B = field.B(np.concatenate([[t], rr]))
+        Bsq = np.dot(B, B)
+        return g * mass / (charge * Bsq) * np.cross(B, v)
+
+    def norm(a):
+        return np.sqrt(np.dot(a, a))
+
+    GC_old = np.array(r) - gyrovector(r)
+    GC_list = [GC_old]
+    it = 1
+    while it <= maxiter:
+        GC = r - gyrovector(GC_old)
+        GC_list.append(GC)
+        if norm(GC - GC_old) / norm(GC) < tol:
+            if debug:
+                return GC_list
+            B = field.B(np.concatenate([[t], GC]))
+            return GC, np.dot(v, B) / norm(B), norm(v)
+        GC_old = GC
+        it += 1
+    print("Could not reach the specified tolerance after ", it, " iterations.")
+
+
+def getperp(v):
+    """rapt/utils.py:328-374."""
+    assert len(v) == 3
+    if v[0] == 0.0 and v[1] == 0.0 and v[2] == 0.0:
+        raise ValueError("Zero vector")
+    if v[0] == 0:
+        return np.array([1, 0, 0])
+    if v[1] == 0:
+        return np.array([0, 1, 0])
+    if v[2] == 0:
+        return np.array([0, 0, 1])
+    cc = -1.0 * (v[0] + v[1]) / v[2]
+    return np.array([1, 1, cc]) / np.sqrt(2 + cc ** 2)
+
+
+def GCtoFP(t, R, vp, speed, field, mass, charge, gyrophase=0):
+    """rapt/utils.py:376-433: particle position and velocity for a guiding centre."""
+    B = field.B(np.concatenate([[t], R]))
+    Bsq = np.dot(B, B)
+    b = B / np.sqrt(Bsq)
+    pa = np.arccos(vp / speed)
+    rc = cyclotron_radius2(t, R, vp, speed, field, mass, charge)
+    u = getperp(B)
+    u = u / np.sqrt(np.dot(u, u))
+    w = np.cross(b, u)
+    s = np.sign(charge)
+    pos = R + rc * (np.cos(gyrophase) * u + np.sin(gyrophase) * w)
+    vel = speed * (np.cos(pa) * b + s * np.sin(pa) * np.sin(gyrophase) * u - s * np.sin(pa) * np.cos(gyrophase) * w)
+    return pos, vel
