@@ -111,6 +111,14 @@ void finish_field(FieldP* f) {
       break;
     default: break;
   }
+  // float-float constants of the FP32 form's field models (positions in Re)
+  double k[4] = {0, 0, 0, 0};
+  if (f->model == RAPT_EARTH_DIPOLE) k[0] = -3.0 * p[0];
+  if (f->model == RAPT_DOUBLE_DIPOLE) { k[0] = -p[0]; k[1] = p[1] / kRe; k[2] = p[2]; }
+  for (int i = 0; i < 4; ++i) {
+    f->dh[i] = (float)k[i];
+    f->dl[i] = (float)(k[i] - (double)f->dh[i]);
+  }
 }
 
 KParams make_params(const Ctx* c, int kind) {
@@ -262,7 +270,10 @@ int rapt_config_set(void* ctx, const rapt_config* g) {
     return fail(c, RAPT_ERR_INVALID, "bad tolerances, nsteps or cyclotronresolution");
   if (g->tableau < 0 || g->tableau > 1) return fail(c, RAPT_ERR_INVALID, "tableau must be 0 or 1");
   if (g->gc_eom < 0 || g->gc_eom > 2) return fail(c, RAPT_ERR_INVALID, "gc_eom must be 0, 1 or 2");
-  if (g->form != RAPT_FORM_PLAIN) return fail(c, RAPT_ERR_UNSUPPORTED, "form %d not available", g->form);
+  if (g->form != RAPT_FORM_PLAIN && g->form != RAPT_FORM_FP32)
+    return fail(c, RAPT_ERR_UNSUPPORTED, "form %d not available", g->form);
+  if (g->form == RAPT_FORM_FP32 && (g->tableau != 0 || g->gc_eom != 0))
+    return fail(c, RAPT_ERR_UNSUPPORTED, "the FP32 form runs DOP853/DOPRI5 with the Tao-Chan-Brizard equations");
   c->cfg = *g;
   return RAPT_OK;
 }
@@ -454,7 +465,9 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
   const int tab = c->cfg.tableau;
   const int block = c->cfg.threads_per_block > 0 ? c->cfg.threads_per_block : 128;
   if (block % 32 != 0 || block > 128) return fail(c, RAPT_ERR_INVALID, "threads_per_block must be a multiple of 32, <= 128");
-  int bps_p = T.occ_particle[tab](block), bps_g = T.occ_gc[tab](block);
+  const bool f32 = c->cfg.form == RAPT_FORM_FP32;
+  int bps_p = f32 ? T.occ_particle32(block) : T.occ_particle[tab](block);
+  int bps_g = f32 ? T.occ_gc32(block) : T.occ_gc[tab](block);
   if (c->cfg.blocks_per_sm > 0) {
     bps_p = std::min(bps_p, c->cfg.blocks_per_sm);
     bps_g = std::min(bps_g, c->cfg.blocks_per_sm);
@@ -474,12 +487,12 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
     LaunchArgs a{E, P, c->scratch, 0, block, s};
     if (kind != RAPT_KIND_GC) {
       a.grid = c->num_sms * bps_p;
-      CK(T.particle[tab](a));
+      CK(f32 ? T.particle32(a) : T.particle[tab](a));
       ++kl;
     }
     if (kind != RAPT_KIND_PARTICLE) {
       a.grid = c->num_sms * bps_g;
-      CK(T.gc[tab](a));
+      CK(f32 ? T.gc32(a) : T.gc[tab](a));
       ++kl;
     }
     ++launches;

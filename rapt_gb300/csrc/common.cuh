@@ -26,6 +26,7 @@ struct FieldP {
   double timestep;    // _Field.timederivstepsize
   double inv2d;       // 1 / (2 gradstep)
   double c0, c1, c2;  // model constants precomputed on the host
+  float dh[4], dl[4]; // float-float model constants (hi, lo) for the FP32 form
 };
 
 // rapt.params plus device options, resolved on the host.

@@ -1,0 +1,445 @@
+// fp32_kernels.cuh -- persistent kernels of the FP32-stage form.
+//
+// Same work distribution, output-interval loop, Adaptive segments and status
+// handling as tracer_kernels.cuh (Particle.py:230-309, GuidingCenter.py:397-458,
+// Adaptive.py:187-222); the RK stages use the float-float arithmetic of fp32_form.cuh. Adiabaticity tests and
+// the particle <-> guiding-centre conversions run in FP64 on the SI state.
+#pragma once
+#include "fp32_form.cuh"
+
+namespace rapt {
+
+template <int M>
+__global__ void __launch_bounds__(128) k_particle32(DevEnsemble E, KParams P, Scratch* S) {
+  int64_t idx = -1;
+  bool exhausted = false;
+  long long budget = P.budget;
+  LaneStats st;
+
+  DF y[6];
+  DF k1[6];
+  double scale[6] = {1, 1, 1, 1, 1, 1};
+  double rt = 0, t_row = 0, tcur = 0, dt = 0, stop = 0, mass = 0, charge = 0, delta = 0, rowt = 0;
+  DF qmc{0.f, 0.f}, qm{0.f, 0.f}, igam{0.f, 0.f};
+  long long nacc = 0, nrej = 0, nfcn = 0;
+  int status = 0, flags = 0, nrows = 0, nsw = 0, nseg = 0, nswitch = 0;
+  bool k1_valid = false, seg_ok = true, in_interval = false;
+  double xend = 0, h = 0, facold_beta = 1, hmax = 0, posneg = 1;
+  bool reject = false, last = false;
+  int nst = 0, nacc_int = 0;
+
+  constexpr double beta = 0.1, safe = 0.9;
+  constexpr double expo1 = 1.0 / 8.0 - beta * 0.2, facc1 = 1.0 / 0.3, facc2 = 1.0 / 6.0;
+
+  auto state_si = [&](double* s) {
+    for (int i = 0; i < 6; ++i) s[i] = df_to_double(y[i]) * scale[i];
+  };
+  auto begin_segment = [&](double seg_delta) {
+    rt = t_row;
+    double s[6];
+    state_si(s);
+    const double gm = sqrt(mass * mass + (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]) / (kC * kC));
+    igam = df_from_double(mass / gm);
+    const double vel[3] = {s[3] / gm, s[4] / gm, s[5] / gm};
+    dt = cyc_period_vel<M>(P.f, t_row, s, vel, mass, charge) / P.cycres;
+    stop = t_row + seg_delta;
+    seg_ok = true;
+    k1_valid = false;
+    in_interval = false;
+  };
+  auto load = [&](int64_t k) {
+    mass = E.mass[k]; charge = E.charge[k]; delta = E.delta[k];
+    const double mc = mass * kC;
+    for (int i = 0; i < 3; ++i) { scale[i] = 1.0; scale[3 + i] = mc; }
+    for (int i = 0; i < 6; ++i) y[i] = df_from_double(E.s[i][k] / scale[i]);
+    qmc = df_from_double(charge / mc);
+    qm = df_from_double(charge / mass);
+    rt = E.t_int[k]; t_row = E.t_row[k]; tcur = E.tcur[k];
+    nacc = E.naccept[k]; nrej = E.nreject[k]; nfcn = E.nfcn[k];
+    status = E.status[k]; flags = E.flags[k]; nrows = E.nrows[k]; nswitch = E.nswitch[k];
+    nseg = E.nseg[k];
+    nsw = nswitch;
+    in_interval = false;
+    k1_valid = false;
+    seg_ok = true;
+    if (E.seg_active[k]) {
+      stop = E.seg_stop[k]; dt = E.seg_dt[k]; igam = df_from_double(mass * E.seg_gm[k]);
+    } else {
+      begin_segment((P.kind == RAPT_KIND_ADAPTIVE && nseg > 0) ? delta - tcur : delta);
+    }
+  };
+  auto store = [&](int64_t k, bool active) {
+    double s[6];
+    state_si(s);
+    for (int i = 0; i < 6; ++i) E.s[i][k] = s[i];
+    E.t_int[k] = rt; E.t_row[k] = t_row; E.tcur[k] = tcur;
+    E.naccept[k] = nacc; E.nreject[k] = nrej; E.nfcn[k] = nfcn;
+    E.status[k] = status; E.flags[k] = flags; E.nrows[k] = nrows; E.nswitch[k] = nswitch; E.nseg[k] = nseg;
+    E.seg_active[k] = active ? 1 : 0;
+    E.seg_stop[k] = stop; E.seg_dt[k] = dt; E.seg_gm[k] = df_to_double(igam) / mass;
+  };
+
+  for (;;) {
+    warp_refill(&S->queue[0], E, RAPT_MODE_PARTICLE, idx, exhausted, load);
+    if (__all_sync(kFull, idx < 0)) break;
+    if (idx < 0) continue;
+
+    const ParticleRHSdf<M> rhs{P.f, qmc, qm, igam, P.enforce_eq != 0};
+    bool release = false;
+
+    if (!in_interval) {
+      if (!(seg_ok && rt < stop)) {
+        bool more = false;
+        if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && tcur < delta) {
+          if (nseg + 1 >= P.max_segments) {
+            status = RAPT_ST_ADAPTIVE_LIMIT;
+          } else {
+            more = true;
+            ++nseg;
+            begin_segment(delta - tcur);
+          }
+        }
+        if (!more) {
+          flags |= RAPT_FLAG_DONE;
+          st.done++;
+          if (status != RAPT_ST_OK) st.fail++;
+          store(idx, false);
+          idx = -1;
+          continue;
+        }
+      }
+      if (budget <= 0) { store(idx, true); idx = -1; exhausted = true; st.pend++; continue; }
+      if (nrows + 2 > P.max_rows) { status = RAPT_ST_ROWS_FULL; store(idx, true); idx = -1; continue; }
+      xend = rt + dt;
+      rowt = rt + dt;
+      hmax = fabs(xend - rt);
+      posneg = copysign(1.0, xend - rt);
+      nst = 0;
+      nacc_int = 0;
+      if (!k1_valid) {
+        rhs(rt, y, k1);
+        k1_valid = true;
+        st.rhs++;
+      }
+      h = hinit_df<6>(rhs, rt, y, k1, scale, posneg, 1.0 / 8.0, hmax, P.rtol, P.atol);
+      st.rhs++;
+      nfcn += 2;
+      facold_beta = powf_fast(1e-4, (float)beta);
+      reject = false;
+      last = false;
+      in_interval = true;
+    }
+
+    bool ended = false;
+    int fail = 0;
+    if (nst > P.nsteps) { ended = true; fail = RAPT_ST_MAXSTEPS; }
+    else if (0.1 * fabs(h) <= fabs(rt) * kUround) { ended = true; fail = RAPT_ST_HMIN; }
+    else {
+      if ((rt + 1.01 * h - xend) * posneg > 0.0) { h = xend - rt; last = true; }
+      ++nst;
+      --budget;
+      DF y1[6];
+      double err;
+      dop853_attempt_df<6>(rhs, rt, y, k1, h, scale, P.rtol, P.atol, y1, err);
+      nfcn += 11;
+      st.rhs += 11;
+      const double fac11 = powf_fast(err, (float)expo1);
+      double fac = fac11 / facold_beta;
+      fac = fmax(facc2, fmin(facc1, fac / safe));
+      double hnew = h / fac;
+      if (err <= 1.0) {
+        facold_beta = powf_fast(fmax(err, 1.0e-4), (float)beta);
+        ++nacc; ++nacc_int; st.acc++;
+        const double xph = rt + h;
+        for (int i = 0; i < 6; ++i) y[i] = y1[i];
+        rhs(xph, y, k1);
+        nfcn += 1;
+        st.rhs++;
+        rt = xph;
+        if (last) {
+          h = hnew;
+          ended = true;
+        } else {
+          if (fabs(hnew) > hmax) hnew = posneg * hmax;
+          if (reject) hnew = posneg * fmin(fabs(hnew), fabs(h));
+          reject = false;
+          h = hnew;
+        }
+      } else {
+        hnew = h / facc1;  // a rejected DOP853 step shrinks by dfactor, as SciPy's dop853 does
+        reject = true;
+        if (nacc_int >= 1) { ++nrej; st.rej++; }
+        last = false;
+        h = hnew;
+      }
+    }
+
+    if (ended) {
+      in_interval = false;
+      double s[6];
+      state_si(s);
+      if (fail) { seg_ok = false; status = fail; }
+      if (!all_finite<6>(s)) { seg_ok = false; status = RAPT_ST_NONFINITE; }
+      t_row = rowt;
+      tcur = rt + dt;
+      put_row(E, P, idx, nrows, rowt, s, 6, RAPT_MODE_PARTICLE);
+      if ((flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE &&
+          particle_isadiabatic<M>(P, t_row, s, mass, charge)) {
+        if (P.kind == RAPT_KIND_ADAPTIVE) {
+          double g[6], mu, vs;
+          if (particle_to_gc<M>(P.f, t_row, s, mass, charge, g, mu, vs)) {
+            for (int i = 0; i < 6; ++i) E.s[i][idx] = g[i];
+            E.mu[idx] = mu;
+            E.v[idx] = vs;
+            E.mode[idx] = RAPT_MODE_GC;
+            tcur = t_row;
+            rt = t_row;
+            ++nseg;
+            if (nsw < P.max_sw) {
+              E.sw_time[(size_t)idx * P.max_sw + nsw] = tcur;
+              E.sw_mode[(size_t)idx * P.max_sw + nsw] = RAPT_MODE_GC;
+            }
+            ++nsw;
+            nswitch = nsw;
+            const double first[6] = {g[0], g[1], g[2], g[3], mu, vs};
+            put_row(E, P, idx, nrows, t_row, first, 6, RAPT_MODE_GC);
+            st.sw++;
+            st.pend++;
+            E.t_int[idx] = rt; E.t_row[idx] = t_row; E.tcur[idx] = tcur;
+            E.naccept[idx] = nacc; E.nreject[idx] = nrej; E.nfcn[idx] = nfcn;
+            E.status[idx] = status; E.flags[idx] = flags; E.nrows[idx] = nrows; E.nswitch[idx] = nswitch;
+            E.nseg[idx] = nseg; E.seg_active[idx] = 0;
+            idx = -1;
+            continue;
+          }
+          status = RAPT_ST_GC_NOCONV;
+          flags |= RAPT_FLAG_DONE;
+          st.done++;
+          st.fail++;
+        } else {
+          flags |= RAPT_FLAG_RAISED | RAPT_FLAG_DONE;
+          st.done++;
+        }
+        release = true;
+      }
+    }
+    if (release) {
+      store(idx, false);
+      idx = -1;
+    }
+  }
+  st.flush(S);
+}
+
+template <int M>
+__global__ void __launch_bounds__(128) k_gc32(DevEnsemble E, KParams P, Scratch* S) {
+  int64_t idx = -1;
+  bool exhausted = false;
+  long long budget = P.budget;
+  LaneStats st;
+
+  DF y[4];
+  DF k1[4];
+  double scale[4] = {1, 1, 1, 1};
+  double rt = 0, t_row = 0, tcur = 0, dt = 0, stop = 0, mass = 0, charge = 0, delta = 0, mu = 0, vs = 0;
+  DF kmu{0.f, 0.f}, mcq{0.f, 0.f}, muq{0.f, 0.f}, qmc{0.f, 0.f};
+  long long nacc = 0, nrej = 0, nfcn = 0;
+  int status = 0, flags = 0, nrows = 0, nsw = 0, nseg = 0, nswitch = 0;
+  bool k1_valid = false, seg_ok = true, in_interval = false;
+  double xend = 0, h = 0, facold_beta = 1, hmax = 0, posneg = 1;
+  bool reject = false, last = false;
+  int nst = 0, nacc_int = 0;
+
+  constexpr double beta = 0.04, safe = 0.9;
+  constexpr double expo1 = 0.2 - beta * 0.75, facc1 = 1.0 / 0.2, facc2 = 1.0 / 10.0;
+
+  auto state_si = [&](double* s) {
+    for (int i = 0; i < 4; ++i) s[i] = df_to_double(y[i]) * scale[i];
+    s[4] = 0.0;
+    s[5] = 0.0;
+  };
+  auto begin_segment = [&](double seg_delta) {
+    rt = t_row;
+    dt = P.gctimestep;
+    stop = t_row + seg_delta;
+    seg_ok = true;
+    if (!(dt > 0.0)) { seg_ok = false; status = RAPT_ST_BAD_INPUT; }
+    k1_valid = false;
+    in_interval = false;
+  };
+  auto load = [&](int64_t k) {
+    mass = E.mass[k]; charge = E.charge[k]; delta = E.delta[k];
+    mu = E.mu[k]; vs = E.v[k];
+    const double mc = mass * kC;
+    scale[0] = scale[1] = scale[2] = 1.0;
+    scale[3] = mc;
+    for (int i = 0; i < 4; ++i) y[i] = df_from_double(E.s[i][k] / scale[i]);
+    kmu = df_from_double(2.0 * mu / (mass * kC * kC));
+    mcq = df_from_double(mc / charge);
+    muq = df_from_double(mu / charge);
+    qmc = df_from_double(charge / mc);
+    rt = E.t_int[k]; t_row = E.t_row[k]; tcur = E.tcur[k];
+    nacc = E.naccept[k]; nrej = E.nreject[k]; nfcn = E.nfcn[k];
+    status = E.status[k]; flags = E.flags[k]; nrows = E.nrows[k]; nswitch = E.nswitch[k];
+    nseg = E.nseg[k];
+    nsw = nswitch;
+    in_interval = false;
+    k1_valid = false;
+    seg_ok = true;
+    if (E.seg_active[k]) {
+      stop = E.seg_stop[k]; dt = E.seg_dt[k];
+    } else {
+      begin_segment((P.kind == RAPT_KIND_ADAPTIVE && nseg > 0) ? delta - tcur : delta);
+    }
+  };
+  auto store = [&](int64_t k, bool active) {
+    double s[6];
+    state_si(s);
+    for (int i = 0; i < 6; ++i) E.s[i][k] = s[i];
+    E.t_int[k] = rt; E.t_row[k] = t_row; E.tcur[k] = tcur;
+    E.naccept[k] = nacc; E.nreject[k] = nrej; E.nfcn[k] = nfcn;
+    E.status[k] = status; E.flags[k] = flags; E.nrows[k] = nrows; E.nswitch[k] = nswitch; E.nseg[k] = nseg;
+    E.seg_active[k] = active ? 1 : 0;
+    E.seg_stop[k] = stop; E.seg_dt[k] = dt;
+  };
+
+  for (;;) {
+    warp_refill(&S->queue[1], E, RAPT_MODE_GC, idx, exhausted, load);
+    if (__all_sync(kFull, idx < 0)) break;
+    if (idx < 0) continue;
+
+    const GcRHSdf<M> rhs{P.f, kmu, mcq, muq, qmc, P.enforce_eq != 0};
+    bool release = false;
+
+    if (!in_interval) {
+      if (!(seg_ok && rt < stop)) {
+        bool more = false;
+        if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_BAD_INPUT &&
+            tcur < delta) {
+          if (nseg + 1 >= P.max_segments) {
+            status = RAPT_ST_ADAPTIVE_LIMIT;
+          } else {
+            more = true;
+            ++nseg;
+            begin_segment(delta - tcur);
+          }
+        }
+        if (!more) {
+          flags |= RAPT_FLAG_DONE;
+          st.done++;
+          if (status != RAPT_ST_OK) st.fail++;
+          store(idx, false);
+          idx = -1;
+          continue;
+        }
+      }
+      if (budget <= 0) { store(idx, true); idx = -1; exhausted = true; st.pend++; continue; }
+      if (nrows + 2 > P.max_rows) { status = RAPT_ST_ROWS_FULL; store(idx, true); idx = -1; continue; }
+      xend = rt + dt;
+      hmax = fabs(xend - rt);
+      posneg = copysign(1.0, xend - rt);
+      nst = 0;
+      nacc_int = 0;
+      if (!k1_valid) {
+        rhs(rt, y, k1);
+        k1_valid = true;
+        st.rhs++;
+      }
+      h = hinit_df<4>(rhs, rt, y, k1, scale, posneg, 1.0 / 5.0, hmax, P.rtol, P.atol);
+      st.rhs++;
+      nfcn += 2;
+      facold_beta = powf_fast(1e-4, (float)beta);
+      reject = false;
+      last = false;
+      in_interval = true;
+    }
+
+    bool ended = false;
+    int fail = 0;
+    if (nst > P.nsteps) { ended = true; fail = RAPT_ST_MAXSTEPS; }
+    else if (0.1 * fabs(h) <= fabs(rt) * kUround) { ended = true; fail = RAPT_ST_HMIN; }
+    else {
+      if ((rt + 1.01 * h - xend) * posneg > 0.0) { h = xend - rt; last = true; }
+      ++nst;
+      --budget;
+      DF y1[4], k7[4];
+      double err;
+      dopri5_attempt_df<4>(rhs, rt, y, k1, h, scale, P.rtol, P.atol, y1, k7, err);
+      nfcn += 6;
+      st.rhs += 6;
+      const double fac11 = powf_fast(err, (float)expo1);
+      double fac = fac11 / facold_beta;
+      fac = fmax(facc2, fmin(facc1, fac / safe));
+      double hnew = h / fac;
+      if (err <= 1.0) {
+        facold_beta = powf_fast(fmax(err, 1.0e-4), (float)beta);
+        ++nacc; ++nacc_int; st.acc++;
+        for (int i = 0; i < 4; ++i) { k1[i] = k7[i]; y[i] = y1[i]; }
+        rt = rt + h;
+        if (last) {
+          h = hnew;
+          ended = true;
+        } else {
+          if (fabs(hnew) > hmax) hnew = posneg * hmax;
+          if (reject) hnew = posneg * fmin(fabs(hnew), fabs(h));
+          reject = false;
+          h = hnew;
+        }
+      } else {
+        hnew = h / fmin(facc1, fac11 / safe);
+        reject = true;
+        if (nacc_int >= 1) { ++nrej; st.rej++; }
+        last = false;
+        h = hnew;
+      }
+    }
+
+    if (ended) {
+      in_interval = false;
+      double s[6];
+      state_si(s);
+      if (fail) { seg_ok = false; status = fail; }
+      if (!all_finite<4>(s)) { seg_ok = false; status = RAPT_ST_NONFINITE; }
+      t_row = rt;
+      tcur = rt;
+      put_row(E, P, idx, nrows, rt, s, 4, RAPT_MODE_GC);
+      if ((flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE &&
+          !gc_isadiabatic<M>(P, t_row, s, mu, mass, charge)) {
+        if (P.kind == RAPT_KIND_ADAPTIVE) {
+          double s6[6];
+          gc_to_particle<M>(P.f, t_row, s, mu, mass, charge, s6);
+          for (int i = 0; i < 6; ++i) E.s[i][idx] = s6[i];
+          E.mode[idx] = RAPT_MODE_PARTICLE;
+          tcur = t_row;
+          rt = t_row;
+          ++nseg;
+          if (nsw < P.max_sw) {
+            E.sw_time[(size_t)idx * P.max_sw + nsw] = tcur;
+            E.sw_mode[(size_t)idx * P.max_sw + nsw] = RAPT_MODE_PARTICLE;
+          }
+          ++nsw;
+          nswitch = nsw;
+          put_row(E, P, idx, nrows, t_row, s6, 6, RAPT_MODE_PARTICLE);
+          st.sw++;
+          st.pend++;
+          E.t_int[idx] = rt; E.t_row[idx] = t_row; E.tcur[idx] = tcur;
+          E.naccept[idx] = nacc; E.nreject[idx] = nrej; E.nfcn[idx] = nfcn;
+          E.status[idx] = status; E.flags[idx] = flags; E.nrows[idx] = nrows; E.nswitch[idx] = nswitch;
+          E.nseg[idx] = nseg; E.seg_active[idx] = 0;
+          idx = -1;
+          continue;
+        }
+        flags |= RAPT_FLAG_RAISED | RAPT_FLAG_DONE;
+        st.done++;
+        release = true;
+      }
+    }
+    if (release) {
+      store(idx, false);
+      idx = -1;
+    }
+  }
+  st.flush(S);
+}
+
+}  // namespace rapt

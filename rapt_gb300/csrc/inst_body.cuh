@@ -1,6 +1,7 @@
 // inst_body.cuh -- instantiates every kernel for one field model. Included by
 // inst_model<k>.cu with RAPT_MODEL defined, so the models compile in parallel.
 #include "eval_kernels.cuh"
+#include "fp32_kernels.cuh"
 #include "launch.h"
 
 #define RAPT_CAT2(a, b) a##b
@@ -32,6 +33,24 @@ int occ_gc(int block) {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc<kM, TAB>, block, 0);
   return nb;
 }
+cudaError_t launch_particle32(const LaunchArgs& a) {
+  k_particle32<kM><<<a.grid, a.block, 0, a.stream>>>(a.E, a.P, a.S);
+  return cudaGetLastError();
+}
+cudaError_t launch_gc32(const LaunchArgs& a) {
+  k_gc32<kM><<<a.grid, a.block, 0, a.stream>>>(a.E, a.P, a.S);
+  return cudaGetLastError();
+}
+int occ_particle32(int block) {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_particle32<kM>, block, 0);
+  return nb;
+}
+int occ_gc32(int block) {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc32<kM>, block, 0);
+  return nb;
+}
 cudaError_t field_eval(const FieldP& f, int what, int64_t n, const double* tpos, double* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   k_field_eval<kM><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(f, what, n, tpos, out);
@@ -59,6 +78,10 @@ void RAPT_CAT(register_model_, RAPT_MODEL)(ModelTable* t) {
   t->occ_particle[1] = occ_particle<1>;
   t->occ_gc[0] = occ_gc<0>;
   t->occ_gc[1] = occ_gc<1>;
+  t->particle32 = launch_particle32;
+  t->gc32 = launch_gc32;
+  t->occ_particle32 = occ_particle32;
+  t->occ_gc32 = occ_gc32;
   t->field_eval = field_eval;
   t->rhs_eval = rhs_eval;
   t->adaptive_init = adaptive_init;

@@ -26,6 +26,8 @@ struct ModelTable {
   LaunchFn gc[2];
   OccFn occ_particle[2];
   OccFn occ_gc[2];
+  LaunchFn particle32, gc32;  // FP32-stage form (DOP853 / DOPRI5)
+  OccFn occ_particle32, occ_gc32;
   FieldEvalFn field_eval;
   RhsEvalFn rhs_eval;
   AdaptiveInitFn adaptive_init;

@@ -140,6 +140,58 @@ __device__ __forceinline__ void dopri5_attempt(const F& f, double x, const doubl
   err = sqrt(e * (1.0 / NV));
 }
 
+// DOPRI5 coefficient table for the rolled stage loop: row s (1..6) gives the
+// stage input y + h sum_j A[s][j] k_{j+1} and its time offset C[s].
+static __constant__ double kDp5A[7][6] = {
+    {0, 0, 0, 0, 0, 0},
+    {dp5::a21, 0, 0, 0, 0, 0},
+    {dp5::a31, dp5::a32, 0, 0, 0, 0},
+    {dp5::a41, dp5::a42, dp5::a43, 0, 0, 0},
+    {dp5::a51, dp5::a52, dp5::a53, dp5::a54, 0, 0},
+    {dp5::a61, dp5::a62, dp5::a63, dp5::a64, dp5::a65, 0},
+    {dp5::a71, 0, dp5::a73, dp5::a74, dp5::a75, dp5::a76}};
+static __constant__ double kDp5C[7] = {0, dp5::c2, dp5::c3, dp5::c4, dp5::c5, 1.0, 1.0};
+
+// The same DOPRI5 attempt with the six right-hand sides in one rolled loop, so
+// that an expensive right-hand side (the guiding-centre stencil) is emitted once
+// rather than six times; stage sums run over all earlier slopes with zero
+// coefficients where the tableau has none.
+template <int NV, class F>
+__device__ __forceinline__ void dopri5_attempt_rolled(const F& f, double x, const double* y, const double* k1,
+                                                      double h, double rtol, double atol, double* y1, double* k7,
+                                                      double& err) {
+  using namespace dp5;
+  double k2[NV], k3[NV], k4[NV], k5[NV], k6[NV], yt[NV], kt[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) { k2[i] = k3[i] = k4[i] = k5[i] = k6[i] = 0.0; }
+#pragma unroll 1
+  for (int s = 1; s <= 6; ++s) {
+    const double* A = kDp5A[s];
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+      yt[i] = y[i] + h * (A[0] * k1[i] + A[1] * k2[i] + A[2] * k3[i] + A[3] * k4[i] + A[4] * k5[i] + A[5] * k6[i]);
+    f(x + kDp5C[s] * h, yt, kt);
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      if (s == 1) k2[i] = kt[i];
+      if (s == 2) k3[i] = kt[i];
+      if (s == 3) k4[i] = kt[i];
+      if (s == 4) k5[i] = kt[i];
+      if (s == 5) k6[i] = kt[i];
+      if (s == 6) { k7[i] = kt[i]; y1[i] = yt[i]; }
+    }
+  }
+  double e = 0.0;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const double ei = (e1 * k1[i] + e3 * k3[i] + e4 * k4[i] + e5 * k5[i] + e6 * k6[i] + e7 * k7[i]) * h;
+    const double sk = atol + rtol * fmax(fabs(y[i]), fabs(y1[i]));
+    const double r = ei / sk;
+    e += r * r;
+  }
+  err = sqrt(e * (1.0 / NV));
+}
+
 // One DOP853 attempt: 11 new stages; the 5th- and 3rd-order error estimates
 // combined as in DOP853. Outputs the 8th-order solution y1 and err.
 template <int NV, class F>

@@ -654,7 +654,7 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
         ++nst;
         --budget;
         double y1[4], k7[4], err;
-        dopri5_attempt<4>(rhs, rt, y, k1, h, P.rtol, P.atol, y1, k7, err);
+        dopri5_attempt_rolled<4>(rhs, rt, y, k1, h, P.rtol, P.atol, y1, k7, err);
         nfcn += 6;
         st.rhs += 6;
         const double fac11 = pow(err, expo1);

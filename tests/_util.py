@@ -42,13 +42,13 @@ def oracle_tracers(O, w, kind):
     return f, cfg, O.tracers_from_structs(out)
 
 
-def gpu_ensemble(w, kind, max_rows=4, max_switch=0, **over):
+def gpu_ensemble(w, kind, max_rows=4, max_switch=0, form=0, **over):
     from rapt_gb300 import Ensemble
     n = len(w["mass"])
     ens = Ensemble(field_of(w), n, max_rows=max_rows, max_switch=max_switch)
     p = dict(w["params"])
     p.update(over)
-    ens.configure(**p)
+    ens.configure(form=form, **p)
     if kind == "gc":
         ens.set_guiding_centers(w["pos"], w["v"], pa=w["pa"], t0=0.0, mass=w["mass"], charge=w["charge"])
     else:

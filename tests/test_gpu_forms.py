@@ -1,0 +1,56 @@
+"""The FP32 form (float-float stages, FP64 time / error norm / step control /
+guiding-centre stencil) against the CPU oracle and against the plain form."""
+import numpy as np
+import pytest
+
+from rapt_gb300 import workloads as W
+from tests._util import gpu_ensemble, rel_state_error, sensitivity_envelope
+
+pytestmark = pytest.mark.gpu
+FP32 = 1
+
+
+def test_fp32_gc_matches_oracle():
+    """Config 2 subsample, 10 s: relative position error <= 5e-6 (target 1e-6),
+    step counts within 1 % of the plain controller's."""
+    w = W.subsample(W.config2(), np.arange(0, 65536, 1024))
+    tr, env_pos, _ = sensitivity_envelope(oracle_mod(), w, "gc", 10.0)
+    ens = gpu_ensemble(w, "gc", max_rows=16, form=FP32)
+    ens.advance("gc", 10.0)
+    h = ens.download()
+    assert np.all(h["status"] == 0)
+    pos, _ = rel_state_error(h["s"], tr["s"], 4)
+    assert pos.max() < 5e-6 and np.median(pos) < 1e-7, (pos.max(), np.median(pos))
+    dpp = np.abs(h["s"][3] - tr["s"][:, 3]) / (w["mass"] * W.c)
+    assert dpp.max() < 1e-4, dpp.max()
+    assert np.max(np.abs(h["naccept"] - tr["naccept"]) / tr["naccept"]) < 0.01
+
+
+def test_fp32_particle_config4_sample():
+    """Config 4 subsample (256 protons and electrons, 50 gyro-periods): relative
+    final-state error and energy drift against the FP64 oracle."""
+    O = oracle_mod()
+    w = W.subsample(W.config4(), np.arange(0, 1048576, 4096))
+    tr, env_pos, env_mom = sensitivity_envelope(O, w, "particle", w["delta"], rel=3e-14)
+    ens = gpu_ensemble(w, "particle", max_rows=1024, form=FP32)
+    ens.advance("particle", w["delta"])
+    h = ens.download()
+    assert np.all(h["status"] == 0)
+    pos, mom = rel_state_error(h["s"], tr["s"], 6)
+    # float-float keeps ~48 bits: bounded by the oracle's own divergence under a
+    # 3e-14 relative start perturbation, floor 1e-9; a start perturbation does
+    # not bound per-operation differences along the few chaotic orbits, hence 97 %
+    within = pos <= np.maximum(1e-9, 100 * env_pos)
+    assert within.mean() >= 0.97, (within.mean(), pos.max())
+    assert np.median(pos) < 1e-11 and np.median(mom) < 1e-9, (np.median(pos), np.median(mom))
+    p0 = np.linalg.norm(w["mass"][:, None] * w["vel"] / np.sqrt(1 - np.sum(w["vel"] ** 2, 1) / W.c ** 2)[:, None],
+                        axis=1)
+    drift_gpu = np.abs(np.linalg.norm(h["s"][3:6].T, axis=1) / p0 - 1)
+    drift_orc = np.abs(np.linalg.norm(tr["s"][:, 3:6], axis=1) / p0 - 1)
+    assert np.median(drift_gpu) <= 2 * np.median(drift_orc) + 1e-12
+
+
+def oracle_mod():
+    from oracle import oracle as O
+    O.lib()
+    return O
