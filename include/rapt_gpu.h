@@ -95,6 +95,8 @@ typedef struct {
   int64_t max_steps_per_launch;  /* per-thread RK-step budget of one launch (0: default) */
   int32_t blocks_per_sm;         /* 0: default */
   int32_t use_graph;             /* 1: replay the launch sequence as a captured CUDA graph */
+  int32_t collect;               /* 1: record step-size training samples (GC, DOPRI5; any form) */
+  double learned_scale;          /* learned forms: multiplier on each MLP step proposal (0: 1) */
 } rapt_config;
 
 /* Host-side SoA view of an ensemble. Any pointer may be NULL on download to
@@ -227,6 +229,37 @@ typedef struct {
 } rapt_gc_device_state;
 int rapt_gc_advance_noalloc(int device, int model, const double* params, int nparams, const rapt_config* cfg,
                             const rapt_gc_device_state* state, double delta, void* stream, rapt_stats* stats);
+
+/* --- step-size / switch MLP (learned forms) ---------------------------------
+ * No counterpart in the reference, whose controllers are SciPy's. A 16 -> 64 ->
+ * 64 -> 2 ReLU network (14 features used, BF16 weights, FP32 accumulation)
+ * proposes a multiplicative correction of the plain controller's next step
+ * (output 0) and the logit of an Adaptive switch (output 1). Parameter vector
+ * (floats): W1T[64][16] b1[64] W2T[64][64] b2[64] W3T[8][64] b3[8] (trainable,
+ * RAPT_MLP_NTRAIN) then feature mean[16], feature scale[16], target mean[8],
+ * target scale[8]. A sample is 18 floats: 16 raw features, the step target
+ * (log of the ideal next step over the controller's), the switch label (-1:
+ * none). Inference and training run on the device (mma.sync BF16). */
+#define RAPT_MLP_NPARAMS 5816
+#define RAPT_MLP_NTRAIN 5768
+#define RAPT_MLP_SAMPLE 18
+int rapt_mlp_set_params(void* ctx, const float* params, int32_t n);
+int rapt_mlp_get_params(void* ctx, float* params, int32_t n);
+/* Batch inference: features[n][16] host -> out[n][2] host (target units). */
+int rapt_mlp_forward(void* ctx, const float* features, int64_t n, float* out);
+/* Gradient of the mean loss over samples[n][18] (host) w.r.t. the trainable
+ * parameters -> grad[RAPT_MLP_NTRAIN] host; loss[2] = (step, switch) parts. */
+int rapt_mlp_grad(void* ctx, const float* samples, int64_t n, float switch_weight, float* grad, double* loss);
+/* Device sample buffer: capacity in samples; an accepted step is sampled when
+ * a hash of (tracer, step count) & mask == 0. Resets the count. */
+int rapt_mlp_samples_reserve(void* ctx, int64_t capacity, uint64_t mask);
+int rapt_mlp_samples_count(void* ctx, int64_t* count);
+int rapt_mlp_samples_download(void* ctx, float* out, int64_t first, int64_t n);
+int rapt_mlp_samples_upload(void* ctx, const float* samples, int64_t n);
+/* Adam (0.9, 0.999, 1e-8) on minibatches drawn from the device samples;
+ * loss[2] = mean (step, switch) loss over the last tenth of the steps. */
+int rapt_mlp_train(void* ctx, int64_t steps, int32_t batch, float lr, float switch_weight, uint64_t seed,
+                   double* loss);
 
 /* Page-lock (pin) a caller-owned host buffer so that uploads and downloads
  * through it run at full PCIe/NVLink-C2C speed; unregister before freeing. */

@@ -32,7 +32,7 @@ class RaptConfig(C.Structure):
                 ("nsteps", C.c_int32), ("rkf_tol", C.c_double), ("rkf_hmin", C.c_double),
                 ("form", C.c_int32), ("threads_per_block", C.c_int32),
                 ("max_steps_per_launch", C.c_int64), ("blocks_per_sm", C.c_int32),
-                ("use_graph", C.c_int32)]
+                ("use_graph", C.c_int32), ("collect", C.c_int32), ("learned_scale", C.c_double)]
 
 
 class RaptHostState(C.Structure):
@@ -78,7 +78,21 @@ SIGNATURES = {
     "rapt_host_unregister": (C.c_int, [_VP]),
     "rapt_gc_advance_noalloc": (C.c_int, [C.c_int, C.c_int, _DP, C.c_int, C.POINTER(RaptConfig), _VP, _D, _VP,
                                           C.POINTER(RaptStats)]),
+    "rapt_mlp_set_params": (C.c_int, [_VP, _VP, C.c_int32]),
+    "rapt_mlp_get_params": (C.c_int, [_VP, _VP, C.c_int32]),
+    "rapt_mlp_forward": (C.c_int, [_VP, _VP, _I64, _VP]),
+    "rapt_mlp_grad": (C.c_int, [_VP, _VP, _I64, C.c_float, _VP, _DP]),
+    "rapt_mlp_samples_reserve": (C.c_int, [_VP, _I64, C.c_uint64]),
+    "rapt_mlp_samples_count": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
+    "rapt_mlp_samples_download": (C.c_int, [_VP, _VP, _I64, _I64]),
+    "rapt_mlp_samples_upload": (C.c_int, [_VP, _VP, _I64]),
+    "rapt_mlp_train": (C.c_int, [_VP, _I64, C.c_int32, C.c_float, C.c_float, C.c_uint64, _DP]),
 }
+
+# Step-size MLP layout (include/rapt_gpu.h RAPT_MLP_*)
+MLP_NPARAMS = 5816
+MLP_NTRAIN = 5768
+MLP_SAMPLE = 18
 
 NOALLOC_MAX_TRACERS = 65536
 
@@ -187,6 +201,56 @@ class Context:
         self.check(self.L.rapt_rhs_eval(self.h, int(mode), n, ptr(state), ptr(mass), ptr(charge), ptr(vv), ptr(out)),
                    "rapt_rhs_eval")
         return out
+
+    # ---- step-size MLP
+    def mlp_set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self.check(self.L.rapt_mlp_set_params(self.h, ptr(p), p.size), "rapt_mlp_set_params")
+
+    def mlp_get_params(self):
+        p = np.zeros(MLP_NPARAMS, np.float32)
+        self.check(self.L.rapt_mlp_get_params(self.h, ptr(p), p.size), "rapt_mlp_get_params")
+        return p
+
+    def mlp_forward(self, features):
+        f = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, 16)
+        out = np.zeros((f.shape[0], 2), np.float32)
+        self.check(self.L.rapt_mlp_forward(self.h, ptr(f), f.shape[0], ptr(out)), "rapt_mlp_forward")
+        return out
+
+    def mlp_grad(self, samples, switch_weight=1.0):
+        s = np.ascontiguousarray(samples, dtype=np.float32).reshape(-1, MLP_SAMPLE)
+        g = np.zeros(MLP_NTRAIN, np.float32)
+        loss = (C.c_double * 2)()
+        self.check(self.L.rapt_mlp_grad(self.h, ptr(s), s.shape[0], float(switch_weight), ptr(g),
+                                        C.cast(loss, _DP)), "rapt_mlp_grad")
+        return g, (loss[0], loss[1])
+
+    def mlp_samples_reserve(self, capacity, mask=0):
+        self.check(self.L.rapt_mlp_samples_reserve(self.h, int(capacity), int(mask)), "rapt_mlp_samples_reserve")
+
+    def mlp_samples_count(self):
+        k = C.c_int64()
+        self.check(self.L.rapt_mlp_samples_count(self.h, C.byref(k)), "rapt_mlp_samples_count")
+        return k.value
+
+    def mlp_samples_download(self, first=0, n=None):
+        if n is None:
+            n = self.mlp_samples_count() - first
+        out = np.zeros((n, MLP_SAMPLE), np.float32)
+        self.check(self.L.rapt_mlp_samples_download(self.h, ptr(out), int(first), int(n)),
+                   "rapt_mlp_samples_download")
+        return out
+
+    def mlp_samples_upload(self, samples):
+        s = np.ascontiguousarray(samples, dtype=np.float32).reshape(-1, MLP_SAMPLE)
+        self.check(self.L.rapt_mlp_samples_upload(self.h, ptr(s), s.shape[0]), "rapt_mlp_samples_upload")
+
+    def mlp_train(self, steps, batch=4096, lr=1e-3, switch_weight=1.0, seed=0):
+        loss = (C.c_double * 2)()
+        self.check(self.L.rapt_mlp_train(self.h, int(steps), int(batch), float(lr), float(switch_weight), int(seed),
+                                         C.cast(loss, _DP)), "rapt_mlp_train")
+        return loss[0], loss[1]
 
     def measure_peaks(self):
         a, b = C.c_double(), C.c_double()

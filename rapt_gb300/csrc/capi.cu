@@ -34,6 +34,18 @@ struct Ctx {
   size_t tmp_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   ModelTable tab[RAPT_N_MODELS];
+  // step-size MLP: one device block of parameters, Adam moments, gradient,
+  // loss and packed weights; a separate sample buffer
+  void* mlp_block = nullptr;
+  float *mlp_p = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_g = nullptr;
+  double* mlp_loss = nullptr;
+  uint32_t* mlp_w = nullptr;
+  bool mlp_ready = false;
+  int64_t mlp_t = 0;  // Adam step count
+  float* samp = nullptr;
+  unsigned long long* samp_count = nullptr;
+  int64_t samp_cap = 0;
+  uint64_t samp_mask = 0;
 };
 
 int fail(Ctx* c, int code, const char* fmt, ...) {
@@ -132,6 +144,14 @@ KParams make_params(const Ctx* c, int kind) {
   P.budget = g.max_steps_per_launch > 0 ? g.max_steps_per_launch : (1LL << 62);
   P.max_rows = c->max_rows; P.max_sw = c->max_sw;
   P.max_segments = 100000;
+  P.mlp_w = c->mlp_w;
+  P.mlp_p = c->mlp_p;
+  P.learn_scale = g.learned_scale > 0 ? (float)g.learned_scale : 1.0f;
+  P.samp = c->samp;
+  P.samp_count = c->samp_count;
+  P.samp_cap = c->samp_cap;
+  P.samp_mask = c->samp_mask;
+  P.collect = g.collect;
   return P;
 }
 
@@ -226,6 +246,8 @@ void rapt_ctx_destroy(void* ctx) {
   cudaFree(c->block);
   cudaFree(c->scratch);
   cudaFree(c->tmp);
+  cudaFree(c->mlp_block);
+  cudaFree(c->samp_count);  // base of the sample allocation
   cudaFreeHost(c->h_pending);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -270,10 +292,13 @@ int rapt_config_set(void* ctx, const rapt_config* g) {
     return fail(c, RAPT_ERR_INVALID, "bad tolerances, nsteps or cyclotronresolution");
   if (g->tableau < 0 || g->tableau > 1) return fail(c, RAPT_ERR_INVALID, "tableau must be 0 or 1");
   if (g->gc_eom < 0 || g->gc_eom > 2) return fail(c, RAPT_ERR_INVALID, "gc_eom must be 0, 1 or 2");
-  if (g->form != RAPT_FORM_PLAIN && g->form != RAPT_FORM_FP32)
+  if (g->form < RAPT_FORM_PLAIN || g->form > RAPT_FORM_LEARNED_FP32)
     return fail(c, RAPT_ERR_UNSUPPORTED, "form %d not available", g->form);
-  if (g->form == RAPT_FORM_FP32 && (g->tableau != 0 || g->gc_eom != 0))
+  if ((g->form == RAPT_FORM_FP32 || g->form == RAPT_FORM_LEARNED_FP32) && (g->tableau != 0 || g->gc_eom != 0))
     return fail(c, RAPT_ERR_UNSUPPORTED, "the FP32 form runs DOP853/DOPRI5 with the Tao-Chan-Brizard equations");
+  if ((g->form == RAPT_FORM_LEARNED || g->form == RAPT_FORM_LEARNED_FP32 || g->collect) && g->tableau != 0)
+    return fail(c, RAPT_ERR_UNSUPPORTED, "the step learner drives the DOPRI5 controller (tableau 0)");
+  if (!(g->learned_scale >= 0)) return fail(c, RAPT_ERR_INVALID, "learned_scale must be >= 0");
   c->cfg = *g;
   return RAPT_OK;
 }
@@ -465,9 +490,16 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
   const int tab = c->cfg.tableau;
   const int block = c->cfg.threads_per_block > 0 ? c->cfg.threads_per_block : 128;
   if (block % 32 != 0 || block > 128) return fail(c, RAPT_ERR_INVALID, "threads_per_block must be a multiple of 32, <= 128");
-  const bool f32 = c->cfg.form == RAPT_FORM_FP32;
+  const int form = c->cfg.form;
+  const bool f32 = form == RAPT_FORM_FP32 || form == RAPT_FORM_LEARNED_FP32;
+  const bool learned = form == RAPT_FORM_LEARNED || form == RAPT_FORM_LEARNED_FP32;
+  const int lrn = learned ? 2 : (c->cfg.collect ? 1 : 0);
+  if (learned && !c->mlp_ready) return fail(c, RAPT_ERR_STATE, "learned form without MLP parameters (rapt_mlp_set_params)");
+  if (c->cfg.collect && !c->samp)
+    return fail(c, RAPT_ERR_STATE, "collection without a sample buffer (rapt_mlp_samples_reserve)");
+  // the step learner drives the guiding-centre kernels; particles run the plain controller
   int bps_p = f32 ? T.occ_particle32(block) : T.occ_particle[tab](block);
-  int bps_g = f32 ? T.occ_gc32(block) : T.occ_gc[tab](block);
+  int bps_g = tab != 0 ? T.occ_gc[tab](block) : (f32 ? T.occ_gc32_lrn[lrn](block) : T.occ_gc_lrn[lrn](block));
   if (c->cfg.blocks_per_sm > 0) {
     bps_p = std::min(bps_p, c->cfg.blocks_per_sm);
     bps_g = std::min(bps_g, c->cfg.blocks_per_sm);
@@ -492,7 +524,7 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
     }
     if (kind != RAPT_KIND_PARTICLE) {
       a.grid = c->num_sms * bps_g;
-      CK(f32 ? T.gc32(a) : T.gc[tab](a));
+      CK(tab != 0 ? T.gc[tab](a) : (f32 ? T.gc32_lrn[lrn](a) : T.gc_lrn[lrn](a)));
       ++kl;
     }
     ++launches;
@@ -583,6 +615,192 @@ int rapt_rhs_eval(void* ctx, int mode, int64_t n, const double* state, const dou
   CK(c->tab[c->field.model].rhs_eval(P, mode, n, d_state, d_mass, d_charge, d_v, d_out, c->stream));
   CK(cudaMemcpyAsync(out, d_out, N * 48, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  return RAPT_OK;
+}
+
+static int mlp_ensure(Ctx* c) {
+  if (c->mlp_block) return RAPT_OK;
+  const size_t fl = (size_t)RAPT_MLP_NPARAMS * 4;
+  const size_t bytes = 4 * fl + 256 + (size_t)kMlpPackedWords * 4;
+  CK(cudaMalloc(&c->mlp_block, bytes));
+  CK(cudaMemsetAsync(c->mlp_block, 0, bytes, c->stream));
+  char* p = static_cast<char*>(c->mlp_block);
+  c->mlp_p = reinterpret_cast<float*>(p);
+  c->mlp_m = reinterpret_cast<float*>(p + fl);
+  c->mlp_v = reinterpret_cast<float*>(p + 2 * fl);
+  c->mlp_g = reinterpret_cast<float*>(p + 3 * fl);
+  c->mlp_loss = reinterpret_cast<double*>(p + 4 * fl);
+  c->mlp_w = reinterpret_cast<uint32_t*>(p + 4 * fl + 256);
+  return RAPT_OK;
+}
+
+int rapt_mlp_set_params(void* ctx, const float* params, int32_t n) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || !params) return RAPT_ERR_INVALID;
+  if (n != RAPT_MLP_NPARAMS) return fail(c, RAPT_ERR_INVALID, "expected %d parameters, got %d", RAPT_MLP_NPARAMS, n);
+  for (int i = RAPT_MLP_NTRAIN + 16; i < RAPT_MLP_NTRAIN + 32; ++i)
+    if (!(params[i] != 0.f) || !std::isfinite(params[i])) return fail(c, RAPT_ERR_INVALID, "feature scales must be finite and nonzero");
+  if (!(params[RAPT_MLP_NTRAIN + 40] != 0.f) || !(params[RAPT_MLP_NTRAIN + 41] != 0.f))
+    return fail(c, RAPT_ERR_INVALID, "target scales must be nonzero");
+  CK(cudaSetDevice(c->device));
+  int rc = mlp_ensure(c);
+  if (rc) return rc;
+  const size_t fl = (size_t)RAPT_MLP_NPARAMS * 4;
+  CK(cudaMemcpyAsync(c->mlp_p, params, fl, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(c->mlp_m, 0, 2 * fl, c->stream));
+  c->mlp_t = 0;
+  CK(mlp_pack(c->mlp_p, c->mlp_w, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->mlp_ready = true;
+  return RAPT_OK;
+}
+
+int rapt_mlp_get_params(void* ctx, float* params, int32_t n) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || !params) return RAPT_ERR_INVALID;
+  if (n != RAPT_MLP_NPARAMS) return fail(c, RAPT_ERR_INVALID, "expected %d parameters, got %d", RAPT_MLP_NPARAMS, n);
+  if (!c->mlp_ready) return fail(c, RAPT_ERR_STATE, "no MLP parameters set");
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(params, c->mlp_p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return RAPT_OK;
+}
+
+int rapt_mlp_forward(void* ctx, const float* features, int64_t n, float* out) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || n < 0 || (n > 0 && (!features || !out))) return RAPT_ERR_INVALID;
+  if (!c->mlp_ready) return fail(c, RAPT_ERR_STATE, "no MLP parameters set");
+  if (n == 0) return RAPT_OK;
+  CK(cudaSetDevice(c->device));
+  const size_t N = (size_t)n;
+  int rc = ensure_tmp(c, N * 18 * 4);
+  if (rc) return rc;
+  float* d_in = static_cast<float*>(c->tmp);
+  float* d_out = d_in + 16 * N;
+  CK(cudaMemcpyAsync(d_in, features, N * 64, cudaMemcpyHostToDevice, c->stream));
+  CK(mlp_forward(c->mlp_w, c->mlp_p, d_in, n, d_out, c->num_sms, c->stream));
+  CK(cudaMemcpyAsync(out, d_out, N * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return RAPT_OK;
+}
+
+int rapt_mlp_grad(void* ctx, const float* samples, int64_t n, float switch_weight, float* grad, double* loss) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || n <= 0 || !samples || !grad) return RAPT_ERR_INVALID;
+  if (!c->mlp_ready) return fail(c, RAPT_ERR_STATE, "no MLP parameters set");
+  CK(cudaSetDevice(c->device));
+  const size_t N = (size_t)n;
+  int rc = ensure_tmp(c, N * RAPT_MLP_SAMPLE * 4);
+  if (rc) return rc;
+  float* d_s = static_cast<float*>(c->tmp);
+  CK(cudaMemcpyAsync(d_s, samples, N * RAPT_MLP_SAMPLE * 4, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(c->mlp_g, 0, (size_t)RAPT_MLP_NTRAIN * 4, c->stream));
+  CK(cudaMemsetAsync(c->mlp_loss, 0, 16, c->stream));
+  CK(mlp_grad(d_s, n, n, 0, 0, 0, switch_weight, c->mlp_w, c->mlp_p, c->mlp_g, c->mlp_loss, c->num_sms, c->stream));
+  CK(cudaMemcpyAsync(grad, c->mlp_g, (size_t)RAPT_MLP_NTRAIN * 4, cudaMemcpyDeviceToHost, c->stream));
+  double hl[2];
+  CK(cudaMemcpyAsync(hl, c->mlp_loss, 16, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (loss) { loss[0] = hl[0]; loss[1] = hl[1]; }
+  return RAPT_OK;
+}
+
+int rapt_mlp_samples_reserve(void* ctx, int64_t capacity, uint64_t mask) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || capacity <= 0) return RAPT_ERR_INVALID;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  if (capacity != c->samp_cap) {
+    cudaFree(c->samp_count);  // base of the sample allocation
+    c->samp = nullptr;
+    c->samp_cap = 0;
+    c->samp_count = nullptr;
+    const size_t bytes = 256 + (size_t)capacity * RAPT_MLP_SAMPLE * 4;
+    void* b = nullptr;
+    if (cudaMalloc(&b, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(c, RAPT_ERR_NOMEM, "cudaMalloc(%zu bytes) for samples failed", bytes);
+    }
+    c->samp_count = static_cast<unsigned long long*>(b);
+    c->samp = reinterpret_cast<float*>(static_cast<char*>(b) + 256);
+    c->samp_cap = capacity;
+  }
+  c->samp_mask = mask;
+  CK(cudaMemsetAsync(c->samp_count, 0, 8, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return RAPT_OK;
+}
+
+static int samples_count(Ctx* c, int64_t* count) {
+  unsigned long long k = 0;
+  CK(cudaMemcpyAsync(&k, c->samp_count, 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *count = (int64_t)std::min<unsigned long long>(k, (unsigned long long)c->samp_cap);
+  return RAPT_OK;
+}
+
+int rapt_mlp_samples_count(void* ctx, int64_t* count) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || !count) return RAPT_ERR_INVALID;
+  if (!c->samp) { *count = 0; return RAPT_OK; }
+  CK(cudaSetDevice(c->device));
+  return samples_count(c, count);
+}
+
+int rapt_mlp_samples_download(void* ctx, float* out, int64_t first, int64_t n) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || first < 0 || n < 0 || (n > 0 && !out)) return RAPT_ERR_INVALID;
+  if (!c->samp) return fail(c, RAPT_ERR_STATE, "no sample buffer");
+  CK(cudaSetDevice(c->device));
+  int64_t cnt = 0;
+  int rc = samples_count(c, &cnt);
+  if (rc) return rc;
+  if (first + n > cnt) return fail(c, RAPT_ERR_INVALID, "samples [%lld, %lld) beyond the %lld held", (long long)first,
+                                   (long long)(first + n), (long long)cnt);
+  if (n == 0) return RAPT_OK;
+  CK(cudaMemcpyAsync(out, c->samp + (size_t)first * RAPT_MLP_SAMPLE, (size_t)n * RAPT_MLP_SAMPLE * 4,
+                     cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return RAPT_OK;
+}
+
+int rapt_mlp_samples_upload(void* ctx, const float* samples, int64_t n) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || n <= 0 || !samples) return RAPT_ERR_INVALID;
+  int rc = rapt_mlp_samples_reserve(ctx, std::max<int64_t>(n, c->samp_cap), c->samp_mask);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(c->samp, samples, (size_t)n * RAPT_MLP_SAMPLE * 4, cudaMemcpyHostToDevice, c->stream));
+  const unsigned long long k = (unsigned long long)n;
+  CK(cudaMemcpyAsync(c->samp_count, &k, 8, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return RAPT_OK;
+}
+
+int rapt_mlp_train(void* ctx, int64_t steps, int32_t batch, float lr, float switch_weight, uint64_t seed,
+                   double* loss) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || steps <= 0 || batch <= 0 || !(lr > 0) || !(switch_weight >= 0)) return RAPT_ERR_INVALID;
+  if (!c->mlp_ready) return fail(c, RAPT_ERR_STATE, "no MLP parameters set");
+  if (!c->samp) return fail(c, RAPT_ERR_STATE, "no samples");
+  CK(cudaSetDevice(c->device));
+  int64_t cnt = 0;
+  int rc = samples_count(c, &cnt);
+  if (rc) return rc;
+  if (cnt <= 0) return fail(c, RAPT_ERR_STATE, "no samples");
+  const int64_t tail = std::max<int64_t>(1, steps / 10);
+  for (int64_t it = 0; it < steps; ++it) {
+    if (it == steps - tail) CK(cudaMemsetAsync(c->mlp_loss, 0, 16, c->stream));
+    CK(cudaMemsetAsync(c->mlp_g, 0, (size_t)RAPT_MLP_NTRAIN * 4, c->stream));
+    CK(mlp_grad(c->samp, cnt, batch, 1, seed, c->mlp_t, switch_weight, c->mlp_w, c->mlp_p, c->mlp_g,
+                it >= steps - tail ? c->mlp_loss : c->mlp_loss + 2, c->num_sms, c->stream));
+    ++c->mlp_t;
+    CK(mlp_adam(c->mlp_p, c->mlp_m, c->mlp_v, c->mlp_g, lr, c->mlp_t, c->stream));
+    CK(mlp_pack(c->mlp_p, c->mlp_w, c->stream));
+  }
+  double hl[2];
+  CK(cudaMemcpyAsync(hl, c->mlp_loss, 16, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (loss) { loss[0] = hl[0] / (double)tail; loss[1] = hl[1] / (double)tail; }
   return RAPT_OK;
 }
 

@@ -38,6 +38,15 @@ struct KParams {
   long long budget;        // RK step attempts per thread per launch
   int max_rows, max_sw;    // per-tracer output capacity
   int max_segments;        // Adaptive: cap on advance() calls per tracer
+  // step-size MLP (learned forms) and training-sample collection
+  const uint32_t* mlp_w;   // packed BF16 weights
+  const float* mlp_p;      // FP32 biases and normalisation
+  float learn_scale;       // multiplier on the learned step proposal
+  float* samp;             // [samp_cap][18] collected samples
+  unsigned long long* samp_count;
+  long long samp_cap;
+  unsigned long long samp_mask;  // an accepted step is sampled when its hash & mask == 0
+  int collect;             // learned kernels: also record samples (on-policy data)
 };
 
 // Device SoA ensemble (all arrays length n unless noted).

@@ -231,12 +231,16 @@ __global__ void __launch_bounds__(128) k_particle32(DevEnsemble E, KParams P, Sc
   st.flush(S);
 }
 
-template <int M>
+template <int M, int LRN = 0>
+// LRN: 0 plain controller, 1 training-sample collection, 2 MLP step proposals.
 __global__ void __launch_bounds__(128) k_gc32(DevEnsemble E, KParams P, Scratch* S) {
   int64_t idx = -1;
   bool exhausted = false;
   long long budget = P.budget;
   LaneStats st;
+  StepLearner<LRN> lr;
+  lr.init();
+  double errold = 1e-4;  // previous accepted error (learner feature)
 
   DF y[4];
   DF k1[4];
@@ -274,6 +278,7 @@ __global__ void __launch_bounds__(128) k_gc32(DevEnsemble E, KParams P, Scratch*
     scale[0] = scale[1] = scale[2] = 1.0;
     scale[3] = mc;
     for (int i = 0; i < 4; ++i) y[i] = df_from_double(E.s[i][k] / scale[i]);
+    lr.load(mass, charge, vs, mc);
     kmu = df_from_double(2.0 * mu / (mass * kC * kC));
     mcq = df_from_double(mc / charge);
     muq = df_from_double(mu / charge);
@@ -306,6 +311,7 @@ __global__ void __launch_bounds__(128) k_gc32(DevEnsemble E, KParams P, Scratch*
   for (;;) {
     warp_refill(&S->queue[1], E, RAPT_MODE_GC, idx, exhausted, load);
     if (__all_sync(kFull, idx < 0)) break;
+    lr.infer(P, h, in_interval);
     if (idx < 0) continue;
 
     const GcRHSdf<M> rhs{P.f, kmu, mcq, muq, qmc, P.enforce_eq != 0};
@@ -345,10 +351,18 @@ __global__ void __launch_bounds__(128) k_gc32(DevEnsemble E, KParams P, Scratch*
         k1_valid = true;
         st.rhs++;
       }
-      h = hinit_df<4>(rhs, rt, y, k1, scale, posneg, 1.0 / 5.0, hmax, P.rtol, P.atol);
-      st.rhs++;
-      nfcn += 2;
+      if (LRN == 2 && lr.have_prop) {
+        // learned first step of the interval instead of HINIT
+        h = posneg * fmin(fabs(h), hmax);
+        lr.have_prop = false;
+        nfcn += 1;
+      } else {
+        h = hinit_df<4>(rhs, rt, y, k1, scale, posneg, 1.0 / 5.0, hmax, P.rtol, P.atol);
+        st.rhs++;
+        nfcn += 2;
+      }
       facold_beta = powf_fast(1e-4, (float)beta);
+      errold = 1e-4;
       reject = false;
       last = false;
       in_interval = true;
@@ -359,7 +373,7 @@ __global__ void __launch_bounds__(128) k_gc32(DevEnsemble E, KParams P, Scratch*
     if (nst > P.nsteps) { ended = true; fail = RAPT_ST_MAXSTEPS; }
     else if (0.1 * fabs(h) <= fabs(rt) * kUround) { ended = true; fail = RAPT_ST_HMIN; }
     else {
-      if ((rt + 1.01 * h - xend) * posneg > 0.0) { h = xend - rt; last = true; }
+      if ((rt + 1.01 * h - xend) * posneg > 0.0) { lr.before_clip(h); h = xend - rt; last = true; }
       ++nst;
       --budget;
       DF y1[4], k7[4];
@@ -367,15 +381,21 @@ __global__ void __launch_bounds__(128) k_gc32(DevEnsemble E, KParams P, Scratch*
       dopri5_attempt_df<4>(rhs, rt, y, k1, h, scale, P.rtol, P.atol, y1, k7, err);
       nfcn += 6;
       st.rhs += 6;
+      lr.on_attempt(P, h, err, last);
       const double fac11 = powf_fast(err, (float)expo1);
       double fac = fac11 / facold_beta;
       fac = fmax(facc2, fmin(facc1, fac / safe));
       double hnew = h / fac;
       if (err <= 1.0) {
+        const double errprev = errold;
+        const bool rej_before = reject;
+        const double hstep = h;
         facold_beta = powf_fast(fmax(err, 1.0e-4), (float)beta);
+        errold = fmax(err, 1.0e-4);
         ++nacc; ++nacc_int; st.acc++;
         for (int i = 0; i < 4; ++i) { k1[i] = k7[i]; y[i] = y1[i]; }
         rt = rt + h;
+        const bool was_last = last;
         if (last) {
           h = hnew;
           ended = true;
@@ -385,6 +405,9 @@ __global__ void __launch_bounds__(128) k_gc32(DevEnsemble E, KParams P, Scratch*
           reject = false;
           h = hnew;
         }
+        lr.on_accept(P, idx, nacc, hstep, err, errprev, h, hmax, was_last, rej_before, nst - nacc_int <= 8,
+                     y[0].hi, y[1].hi, y[2].hi,
+                     y[3].hi, vs, 1.0 - (xend - rt) / hmax);
       } else {
         hnew = h / fmin(facc1, fac11 / safe);
         reject = true;

@@ -51,6 +51,33 @@ int occ_gc32(int block) {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc32<kM>, block, 0);
   return nb;
 }
+// guiding-centre kernels with the step learner; dynamic shared memory per warp
+template <int LRN>
+size_t lrn_smem(int block) {
+  return (size_t)(block / 32) * StepLearner<LRN>::kWarpWords * sizeof(uint32_t);
+}
+template <int LRN>
+cudaError_t launch_gc_lrn(const LaunchArgs& a) {
+  k_gc<kM, 0, LRN><<<a.grid, a.block, lrn_smem<LRN>(a.block), a.stream>>>(a.E, a.P, a.S);
+  return cudaGetLastError();
+}
+template <int LRN>
+cudaError_t launch_gc32_lrn(const LaunchArgs& a) {
+  k_gc32<kM, LRN><<<a.grid, a.block, lrn_smem<LRN>(a.block), a.stream>>>(a.E, a.P, a.S);
+  return cudaGetLastError();
+}
+template <int LRN>
+int occ_gc_lrn(int block) {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc<kM, 0, LRN>, block, lrn_smem<LRN>(block));
+  return nb;
+}
+template <int LRN>
+int occ_gc32_lrn(int block) {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc32<kM, LRN>, block, lrn_smem<LRN>(block));
+  return nb;
+}
 cudaError_t field_eval(const FieldP& f, int what, int64_t n, const double* tpos, double* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   k_field_eval<kM><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(f, what, n, tpos, out);
@@ -82,6 +109,18 @@ void RAPT_CAT(register_model_, RAPT_MODEL)(ModelTable* t) {
   t->gc32 = launch_gc32;
   t->occ_particle32 = occ_particle32;
   t->occ_gc32 = occ_gc32;
+  t->gc_lrn[0] = launch_gc<0>;
+  t->gc_lrn[1] = launch_gc_lrn<1>;
+  t->gc_lrn[2] = launch_gc_lrn<2>;
+  t->occ_gc_lrn[0] = occ_gc<0>;
+  t->occ_gc_lrn[1] = occ_gc_lrn<1>;
+  t->occ_gc_lrn[2] = occ_gc_lrn<2>;
+  t->gc32_lrn[0] = launch_gc32;
+  t->gc32_lrn[1] = launch_gc32_lrn<1>;
+  t->gc32_lrn[2] = launch_gc32_lrn<2>;
+  t->occ_gc32_lrn[0] = occ_gc32;
+  t->occ_gc32_lrn[1] = occ_gc32_lrn<1>;
+  t->occ_gc32_lrn[2] = occ_gc32_lrn<2>;
   t->field_eval = field_eval;
   t->rhs_eval = rhs_eval;
   t->adaptive_init = adaptive_init;

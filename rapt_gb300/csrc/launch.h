@@ -28,10 +28,24 @@ struct ModelTable {
   OccFn occ_gc[2];
   LaunchFn particle32, gc32;  // FP32-stage form (DOP853 / DOPRI5)
   OccFn occ_particle32, occ_gc32;
+  // guiding-centre DOPRI5 kernels with the step learner: [0] plain, [1] sample
+  // collection, [2] MLP proposals; FP64 and FP32-stage forms
+  LaunchFn gc_lrn[3], gc32_lrn[3];
+  OccFn occ_gc_lrn[3], occ_gc32_lrn[3];
   FieldEvalFn field_eval;
   RhsEvalFn rhs_eval;
   AdaptiveInitFn adaptive_init;
 };
+
+// MLP kernels (mlp.cu); packed BF16 weights take kMlpPackedWords u32
+constexpr int kMlpPackedWords = 64 * 8 + 64 * 32 + 8 * 32 + 64 * 32 + 64 * 4;
+cudaError_t mlp_pack(const float* p, uint32_t* w, cudaStream_t s);
+cudaError_t mlp_grad(const float* samples, int64_t nsamp, int64_t batch, int random, uint64_t seed, int64_t step,
+                     float switch_weight, const uint32_t* w, const float* p, float* grad, double* loss, int num_sms,
+                     cudaStream_t s);
+cudaError_t mlp_adam(float* p, float* m, float* v, const float* g, float lr, int64_t t, cudaStream_t s);
+cudaError_t mlp_forward(const uint32_t* w, const float* p, const float* feat, int64_t n, float* out, int num_sms,
+                        cudaStream_t s);
 
 void register_model_0(ModelTable*);
 void register_model_1(ModelTable*);

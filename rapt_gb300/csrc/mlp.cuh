@@ -1,0 +1,311 @@
+// mlp.cuh -- the step-size / switch MLP: 16 (14 used) -> 64 -> 64 -> 2, ReLU,
+// BF16 weights and activations, FP32 accumulation on the tensor cores
+// (mma.sync.m16n8k16.bf16; one warp handles 32 samples at a time).
+//
+// Fragment layouts of mma.m16n8k16 (PTX ISA), g = lane / 4, q = lane % 4:
+//   A (16x16, row): a0 = A[g][2q..2q+1], a1 = A[g+8][2q..], a2 = A[g][2q+8..], a3 = A[g+8][2q+8..]
+//   B (16x8, col):  b0 = B[2q..2q+1][g], b1 = B[2q+8..2q+9][g]
+//   C (16x8):       c0,c1 = C[g][2q..2q+1], c2,c3 = C[g+8][2q..2q+1]
+// Activations go through shared memory as BF16 so that few registers stay
+// live inside the tracer kernels that call the network once per RK step.
+//
+// Output 0 is the log correction of the plain controller's next step size,
+// output 1 the logit of "the next adiabaticity check fails" (Adaptive switch).
+#pragma once
+#include <cuda_bf16.h>
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace rapt {
+
+constexpr int kMlpIn = 16;
+constexpr int kSampleStride = 18;  // 16 features, step target, switch label (-1: none)
+// FP32 parameter vector (offsets in floats); W?T are [out][in]
+constexpr int kOffW1 = 0;                      // W1T [64][16]
+constexpr int kOffB1 = kOffW1 + 64 * 16;
+constexpr int kOffW2 = kOffB1 + 64;            // W2T [64][64]
+constexpr int kOffB2 = kOffW2 + 64 * 64;
+constexpr int kOffW3 = kOffB2 + 64;            // W3T [8][64], rows 2..7 stay zero
+constexpr int kOffB3 = kOffW3 + 8 * 64;
+constexpr int kMlpTrainable = kOffB3 + 8;      // 5768 weights and biases
+constexpr int kOffXmu = kMlpTrainable;         // feature mean [16]
+constexpr int kOffXsig = kOffXmu + 16;         // feature scale [16]
+constexpr int kOffYmu = kOffXsig + 16;         // target mean [8]
+constexpr int kOffYsig = kOffYmu + 8;          // target scale [8]
+constexpr int kMlpParams = kOffYsig + 8;       // 5816 floats
+static_assert(kMlpParams == RAPT_MLP_NPARAMS && kMlpTrainable == RAPT_MLP_NTRAIN, "MLP layout");
+// packed BF16 weights (one u32 = two bf16), offsets in u32
+constexpr int kPW1 = 0;                        // W1T [64][8]
+constexpr int kPW2 = kPW1 + 64 * 8;            // W2T [64][32]
+constexpr int kPW3 = kPW2 + 64 * 32;           // W3T [8][32]
+constexpr int kPW2N = kPW3 + 8 * 32;           // W2  [64 in][32]: B operand of the backward pass
+constexpr int kPW3N = kPW2N + 64 * 32;         // W3  [64 in][4]
+constexpr int kMlpPacked = kPW3N + 64 * 4;
+
+extern __shared__ __align__(16) uint32_t rapt_dyn_smem[];
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+__device__ __forceinline__ float bf16_lo(uint32_t u) { return __uint_as_float(u << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
+
+__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// A fragment (m-tile t, k-step s) of a row-major BF16 matrix stored as u32 [rows][K2].
+__device__ __forceinline__ void load_a(const uint32_t* M, int K2, int t, int s, int g, int q, uint32_t* a) {
+  const int r0 = 16 * t + g, r1 = r0 + 8, c = 8 * s + q;
+  a[0] = M[r0 * K2 + c];
+  a[1] = M[r1 * K2 + c];
+  a[2] = M[r0 * K2 + c + 4];
+  a[3] = M[r1 * K2 + c + 4];
+}
+// B fragment (n-tile j, k-step s) of a K x N matrix stored column-major, u32 [N][K2].
+__device__ __forceinline__ void load_b(const uint32_t* BT, int K2, int j, int s, int g, int q, uint32_t* b) {
+  const int r = 8 * j + g, c = 8 * s + q;
+  b[0] = BT[r * K2 + c];
+  b[1] = BT[r * K2 + c + 4];
+}
+
+// Dense layer out = ReLU(in @ W + b) for 32 rows: in u32 [32][K/2], W as W^T
+// u32 [N][K/2]; writes BF16 out u32 [32][N/2].
+template <int K, int N>
+__device__ __forceinline__ void dense_relu(const uint32_t* in, const uint32_t* WT, const float* bias, uint32_t* out,
+                                           int g, int q) {
+#pragma unroll
+  for (int j = 0; j < N / 8; ++j) {
+    float c[2][4];
+    const float b0 = bias[8 * j + 2 * q], b1 = bias[8 * j + 2 * q + 1];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) { c[t][0] = c[t][2] = b0; c[t][1] = c[t][3] = b1; }
+#pragma unroll
+    for (int s = 0; s < K / 16; ++s) {
+      uint32_t b[2];
+      load_b(WT, K / 2, j, s, g, q, b);
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        uint32_t a[4];
+        load_a(in, K / 2, t, s, g, q, a);
+        mma_bf16(c[t], a, b);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      out[(16 * t + g) * (N / 2) + 4 * j + q] = pack_bf16x2(fmaxf(c[t][0], 0.f), fmaxf(c[t][1], 0.f));
+      out[(16 * t + g + 8) * (N / 2) + 4 * j + q] = pack_bf16x2(fmaxf(c[t][2], 0.f), fmaxf(c[t][3], 0.f));
+    }
+  }
+}
+
+// Output layer (8 columns, two used): this lane's sample's two outputs (network units).
+__device__ __forceinline__ void dense_out(const uint32_t* in, const uint32_t* WT, const float* bias, int g, int q,
+                                          int lane, float* y) {
+  float c[2][4];
+  const float b0 = bias[2 * q], b1 = bias[2 * q + 1];
+#pragma unroll
+  for (int t = 0; t < 2; ++t) { c[t][0] = c[t][2] = b0; c[t][1] = c[t][3] = b1; }
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    uint32_t b[2];
+    load_b(WT, 32, 0, s, g, q, b);
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      uint32_t a[4];
+      load_a(in, 32, t, s, g, q, a);
+      mma_bf16(c[t], a, b);
+    }
+  }
+  // sample 16 t + rr sits on lane 4 (rr % 8), columns 0..1, in c[t][0..1] (rr < 8) or c[t][2..3]
+  const int rr = lane & 15, src = 4 * (rr & 7);
+  float v[2][4];
+#pragma unroll
+  for (int tt = 0; tt < 2; ++tt)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[tt][i] = __shfl_sync(kFull, c[tt][i], src);
+  const bool hi_t = lane >= 16, hi_r = rr >= 8;
+  y[0] = hi_t ? (hi_r ? v[1][2] : v[1][0]) : (hi_r ? v[0][2] : v[0][0]);
+  y[1] = hi_t ? (hi_r ? v[1][3] : v[1][1]) : (hi_r ? v[0][3] : v[0][1]);
+}
+
+// Normalise 16 raw features and write them as BF16 row `lane` of X (u32 [32][8]).
+__device__ __forceinline__ void stage_features(const float* p, const float* f, uint32_t* X, int lane) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const float a = (f[2 * i] - p[kOffXmu + 2 * i]) / p[kOffXsig + 2 * i];
+    const float b = (f[2 * i + 1] - p[kOffXmu + 2 * i + 1]) / p[kOffXsig + 2 * i + 1];
+    X[lane * 8 + i] = pack_bf16x2(a, b);
+  }
+}
+
+// Per-warp shared memory of inference (u32): X [32][8], H1 [32][32], H2 [32][32].
+constexpr int kWarpSmemInfer = 32 * 8 + 32 * 32 + 32 * 32;
+
+// Whole-warp inference on the staged X rows; every lane gets its row's two
+// outputs in target units. All 32 lanes must call it (mma.sync).
+__device__ __forceinline__ void mlp_forward_staged(const uint32_t* w, const float* p, uint32_t* sm, float* out) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+  uint32_t* X = sm;
+  uint32_t* H1 = X + 32 * 8;
+  uint32_t* H2 = H1 + 32 * 32;
+  __syncwarp();
+  dense_relu<16, 64>(X, w + kPW1, p + kOffB1, H1, g, q);
+  __syncwarp();
+  dense_relu<64, 64>(H1, w + kPW2, p + kOffB2, H2, g, q);
+  __syncwarp();
+  float y[2];
+  dense_out(H2, w + kPW3, p + kOffB3, g, q, lane, y);
+  __syncwarp();
+  out[0] = y[0] * p[kOffYsig] + p[kOffYmu];
+  out[1] = y[1] * p[kOffYsig + 1] + p[kOffYmu + 1];
+}
+
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+// ---------------------------------------------------------------- step learner
+// The training target is the step h* = h (1 / err)^(1/5) that would have put the
+// error estimate (order 5) exactly at the acceptance threshold; the host scales
+// the proposals down by a margin calibrated on held-out samples.
+constexpr float kLearnRho = 1.0f;
+constexpr double kMe = 9.10938291e-31;
+
+// Hook of the tracer kernels. LRN = 0: plain (all no-ops), 1: collect training
+// samples from the plain controller, 2: MLP step proposals.
+template <int LRN>
+struct StepLearner {
+  // shared memory per warp: inference buffers (LRN 2), then raw feature rows of
+  // the samples being collected
+  static constexpr int kRawOff = LRN == 2 ? kWarpSmemInfer : 0;
+  static constexpr int kWarpWords = LRN == 0 ? 0 : kRawOff + 32 * 16;
+  float c_mass, c_energy, c_sign, c_pitch;  // per-tracer feature constants
+  float rcap;                               // cap on the learned correction
+  double hbase;                             // collect: the controller's step after the sampled step
+  double hcont;                             // learned: the step wanted before the interval-end clip
+  bool want, pend, have_prop;
+  uint32_t* sm;
+
+  __device__ __forceinline__ void init() {
+    want = pend = have_prop = false;
+    sm = LRN ? rapt_dyn_smem + (threadIdx.x >> 5) * kWarpWords : nullptr;
+  }
+  // Per-tracer constants; vs is the speed, pitch scale converts ppar to cos(pitch).
+  __device__ __forceinline__ void load(double mass, double charge, double vs, double ppar_unit) {
+    want = pend = have_prop = false;
+    if constexpr (LRN != 0) {
+      const double gam = 1.0 / sqrt(1.0 - (vs / kC) * (vs / kC));
+      c_mass = log10f((float)(mass / kMe));
+      c_energy = log10f(fmaxf((float)(gam - 1.0), 1e-12f));
+      c_sign = charge > 0 ? 1.f : -1.f;
+      c_pitch = (float)(ppar_unit / (gam * mass * vs));
+    }
+  }
+  // The step h is about to be clipped to end the output interval.
+  __device__ __forceinline__ void before_clip(double h) {
+    if constexpr (LRN == 2) hcont = h;
+  }
+  // After an accepted step of size h (err, previous err, the controller's next
+  // step hnew) ending at position pos with parallel momentum ppar. A step that
+  // ended an output interval gives no sample; the learned form continues the
+  // next interval with the step wanted before the clip (in place of HINIT).
+  // `allow` switches the proposals off (the plain controller takes over) for
+  // the rest of an output interval that has seen many rejections.
+  __device__ __forceinline__ void on_accept(const KParams& P, int64_t idx, long long nacc, double h, double err,
+                                            double errprev, double& hnew, double hmax, bool last, bool rej_before,
+                                            bool allow, float x, float y, float z, float ppar, double vs,
+                                            double progress) {
+    if constexpr (LRN == 0) return;
+    if (last) {
+      if constexpr (LRN == 2) {
+        hnew = hcont;
+        have_prop = true;
+      }
+      return;
+    }
+    const bool coll = (LRN == 1 || P.collect) &&
+                      (mix64((uint64_t)idx * 0x100000001b3ull + (uint64_t)nacc) & P.samp_mask) == 0;
+    const bool inf = LRN == 2 && allow;
+    if (!coll && !inf) return;
+    float f[16];
+    const float r = sqrtf(x * x + y * y + z * z);
+    f[0] = __logf((float)(fabs(h) * vs) / r);
+    f[1] = __log10f(fmaxf((float)err, 1e-10f));
+    f[2] = __log10f(fmaxf((float)errprev, 1e-10f));
+    f[3] = __logf((float)fabs(hnew / h));
+    f[4] = 1.f;
+    f[5] = c_sign;
+    f[6] = c_mass;
+    f[7] = c_energy;
+    f[8] = ppar * c_pitch;
+    f[9] = __logf(r * (float)(1.0 / kRe));
+    f[10] = z / r;
+    f[11] = (float)progress;
+    f[12] = (float)(hmax / fabs(h));
+    f[13] = rej_before ? 1.f : 0.f;
+    f[14] = 0.f;
+    f[15] = 0.f;
+    const int lane = threadIdx.x & 31;
+    if (coll) {
+      float* row = reinterpret_cast<float*>(sm + kRawOff) + lane * 16;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) row[i] = f[i];
+      pend = true;
+      hbase = hnew;
+    }
+    if constexpr (LRN == 2) {
+      if (inf) {
+        stage_features(P.mlp_p, f, sm, lane);
+        want = true;
+        float cap = (float)(hmax / fabs(hnew));
+        if (rej_before) cap = fminf(cap, (float)(fabs(h) / fabs(hnew)));
+        rcap = cap;
+      }
+    }
+  }
+  // Collect: label the staged sample with the attempt that followed it.
+  __device__ __forceinline__ void on_attempt(const KParams& P, double h, double err, bool clipped) {
+    if constexpr (LRN != 0) {
+      if (!pend) return;
+      pend = false;
+      if (clipped) return;
+      const float y0 = __logf((float)fabs(h / hbase)) + 0.2f * __logf(kLearnRho / fmaxf((float)err, 1e-10f));
+      const unsigned long long pos = atomicAdd(P.samp_count, 1ull);
+      if (pos < (unsigned long long)P.samp_cap) {
+        const float* row = reinterpret_cast<const float*>(sm + kRawOff) + (threadIdx.x & 31) * 16;
+        float* dst = P.samp + pos * kSampleStride;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) dst[i] = row[i];
+        dst[16] = y0;
+        dst[17] = -1.f;
+      }
+    }
+  }
+  // Learned: warp-collective inference for the lanes that staged features;
+  // scales their next step h. Called by all 32 lanes at the top of the loop.
+  __device__ __forceinline__ void infer(const KParams& P, double& h, bool in_interval) {
+    if constexpr (LRN == 2) {
+      if (__any_sync(kFull, want)) {
+        float o[2];
+        mlp_forward_staged(P.mlp_w, P.mlp_p, sm, o);
+        if (want) {
+          const float r = fminf(__expf(fminf(fmaxf(o[0], -3.f), 3.f)) * P.learn_scale, rcap);
+          h *= (double)r;
+        }
+      }
+      want = false;
+    }
+  }
+};
+
+}  // namespace rapt

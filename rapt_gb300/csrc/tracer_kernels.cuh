@@ -19,6 +19,7 @@
 // each output row. Every loop is bounded: nsteps per interval, the per-launch
 // step budget, 20 guiding-centre iterations, and the Adaptive segment cap.
 #pragma once
+#include "mlp.cuh"
 #include "rhs.cuh"
 #include "steppers.cuh"
 
@@ -513,12 +514,18 @@ __global__ void __launch_bounds__(128) k_particle(DevEnsemble E, KParams P, Scra
 
 // ---------------------------------------------------------------- guiding-centre kernel
 // TAB 0: DOPRI5 (GuidingCenter.py:450, SciPy defaults; beta 0 -> 0.04); TAB 1: RKF45.
-template <int M, int TAB>
+// LRN (DOPRI5 only): 0 plain, 1 training-sample collection, 2 MLP step proposals
+// (a proposal replaces the controller's next step after an accepted step and
+// HINIT at the next interval; a rejected proposal falls back to the controller).
+template <int M, int TAB, int LRN = 0>
 __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S) {
+  static_assert(LRN == 0 || TAB == 0, "the step learner drives the DOPRI5 controller");
   int64_t idx = -1;
   bool exhausted = false;
   long long budget = P.budget;
   LaneStats st;
+  StepLearner<LRN> lr;
+  lr.init();
 
   double y[4] = {0, 0, 0, 0}, k1[4] = {0, 0, 0, 0};
   double rt = 0, t_row = 0, tcur = 0, dt = 0, stop = 0, mass = 0, charge = 0, delta = 0, mu = 0, vs = 0;
@@ -568,6 +575,7 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
     } else {
       begin_segment((P.kind == RAPT_KIND_ADAPTIVE && nseg > 0) ? delta - tcur : delta);
     }
+    lr.load(mass, charge, vs, 1.0);
   };
 
   auto store = [&](int64_t k, bool active) {
@@ -585,6 +593,7 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
   for (;;) {
     warp_refill(&S->queue[1], E, RAPT_MODE_GC, idx, exhausted, load);
     if (__all_sync(kFull, idx < 0)) break;
+    lr.infer(P, h, in_interval);
     if (idx < 0) continue;
 
     const GcRHS<M> rhs{P.f, charge, qinv, mu, minv, kmu, inv_mc, igv, gmv, gmv2, P.gc_eom, P.enforce_eq != 0};
@@ -632,9 +641,16 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
       nacc_int = 0;
       if (TAB == 0) {
         if (!k1_valid) { rhs(rt, y, k1); k1_valid = true; st.rhs++; }
-        h = hinit<4>(rhs, rt, y, k1, posneg, 1.0 / 5.0, hmax, P.rtol, P.atol);
-        st.rhs++;
-        nfcn += 2;
+        if (LRN == 2 && lr.have_prop) {
+          // learned first step of the interval instead of HINIT
+          h = posneg * fmin(fabs(h), hmax);
+          lr.have_prop = false;
+          nfcn += 1;
+        } else {
+          h = hinit<4>(rhs, rt, y, k1, posneg, 1.0 / 5.0, hmax, P.rtol, P.atol);
+          st.rhs++;
+          nfcn += 2;
+        }
         facold = 1e-4;
         reject = false;
         last = false;
@@ -650,23 +666,28 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
       if (nst > P.nsteps) { ended = true; fail = RAPT_ST_MAXSTEPS; }
       else if (0.1 * fabs(h) <= fabs(rt) * kUround) { ended = true; fail = RAPT_ST_HMIN; }
       else {
-        if ((rt + 1.01 * h - xend) * posneg > 0.0) { h = xend - rt; last = true; }
+        if ((rt + 1.01 * h - xend) * posneg > 0.0) { lr.before_clip(h); h = xend - rt; last = true; }
         ++nst;
         --budget;
         double y1[4], k7[4], err;
         dopri5_attempt_rolled<4>(rhs, rt, y, k1, h, P.rtol, P.atol, y1, k7, err);
         nfcn += 6;
         st.rhs += 6;
+        lr.on_attempt(P, h, err, last);
         const double fac11 = pow(err, expo1);
         double fac = fac11 / pow(facold, beta);
         fac = fmax(facc2, fmin(facc1, fac / safe));
         double hnew = h / fac;
         if (err <= 1.0) {
+          const double errprev = facold;
+          const bool rej_before = reject;
+          const double hstep = h;
           facold = fmax(err, 1.0e-4);
           ++nacc; ++nacc_int; st.acc++;
 #pragma unroll
           for (int i = 0; i < 4; ++i) { k1[i] = k7[i]; y[i] = y1[i]; }
           rt = rt + h;
+          const bool was_last = last;
           if (last) {
             h = hnew;
             ended = true;
@@ -676,6 +697,9 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
             reject = false;
             h = hnew;
           }
+          lr.on_accept(P, idx, nacc, hstep, err, errprev, h, hmax, was_last, rej_before, nst - nacc_int <= 8,
+                     (float)y[0], (float)y[1],
+                       (float)y[2], (float)y[3], vs, 1.0 - (xend - rt) / hmax);
         } else {
           hnew = h / fmin(facc1, fac11 / safe);
           reject = true;

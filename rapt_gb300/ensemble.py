@@ -154,9 +154,32 @@ class Ensemble:
     # ----------------------------------------------------------- running
     def configure(self, **cfg):
         """Set solver options; keys of rapt_config (rtol, atol, cyclotronresolution,
-        gctimestep, epss, epst, enforce_equatorial, tableau, gc_eom, nsteps, form, ...)."""
-        self.config = dict(cfg)
-        self.ctx.set_config(**cfg)
+        gctimestep, epss, epst, enforce_equatorial, tableau, gc_eom, nsteps, form,
+        collect, learned_scale, ...). Keys not given keep their earlier values."""
+        merged = dict(self.config)
+        merged.update(cfg)
+        self.ctx.set_config(**merged)
+        self.config = merged
+
+    @classmethod
+    def from_workload(cls, w, kind, max_rows=4, max_switch=0, ctx=None, pinned=False, **over):
+        """Ensemble of a workload dict of ``rapt_gb300.workloads`` (field, params,
+        positions and velocities or speeds and pitch angles), uploaded."""
+        from . import fields as F
+        name, kw = w["field"]
+        ens = cls(getattr(F, name)(**kw), len(w["mass"]), max_rows=max_rows, max_switch=max_switch, ctx=ctx,
+                  pinned=pinned)
+        p = dict(w["params"])
+        p.update(over)
+        ens.configure(**p)
+        if kind == "gc":
+            ens.set_guiding_centers(w["pos"], w["v"], pa=w["pa"], t0=0.0, mass=w["mass"], charge=w["charge"])
+        else:
+            ens.set_particles(w["pos"], w["vel"], 0.0, w["mass"], w["charge"])
+        ens.upload()
+        if kind == "adaptive":
+            ens.adaptive_init()
+        return ens
 
     def adaptive_init(self):
         """Adaptive.__init__ mode pick on the device (rapt/Adaptive.py:95-104)."""
