@@ -7,9 +7,14 @@ equatorial pitch 15-85 deg, seed 0), Tao-Chan-Brizard guiding-centre
 equations, DOPRI5 at rtol = atol = 1e-8, GCtimestep 1 s. One step = one
 ``GuidingCenter.advance(1.0)`` of every tracer (one output interval).
 
-``value`` is whole-job accepted steps / device time with the state resident in
-HBM; ``e2e`` is the same metric through the public API with the state copied
-from pinned host memory and back inside the timed region. ``--impl reference``
+Four forms run on the same start state: plain FP64, FP32 stages, learned
+(FP64 with MLP step proposals) and learned+FP32. The step MLP is trained first
+(untimed) on guiding centres of an independent config-2 draw. ``value`` is the
+learned+FP32 form's whole-job accepted steps / device time with the state
+resident in HBM; ``forms`` holds every form's accepted steps/s, rejections,
+right-hand sides, simulated tracer-seconds/s and gyro-periods/s. ``e2e`` is
+the learned+FP32 metric through the public API with the state copied from
+pinned host memory and back inside the timed region. ``--impl reference``
 times the CPU restatement of the reference algorithm (the oracle) on all host
 cores over a bounded sample of the same workload.
 """
@@ -153,7 +158,7 @@ def run_reference(args, rank, ws, dist):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    n = args.cpu_sample or 4096
+    n = args.cpu_sample or 16384
     vals = []
     for i in range(args.warmup + args.steps):
         v, acc, dt = cpu_baseline(n, threads)
@@ -174,47 +179,95 @@ def run_reference(args, rank, ws, dist):
     print(json.dumps(line), flush=True)
 
 
+FORMS = (("plain", 0), ("fp32", 1), ("learned", 2), ("learned_fp32", 3))
+HEADLINE = "learned_fp32"
+
+
+def gyro_frequency_sum(w, magB):
+    """Sum over tracers of 1 / cyclotron period (utils.cyclotron_period) at the start."""
+    c = 299792458.0
+    gamma = 1.0 / np.sqrt(1.0 - (w["v"] / c) ** 2)
+    return float(np.sum(np.abs(w["charge"]) * magB / (2 * np.pi * gamma * w["mass"])))
+
+
+def train_step_model(ctx, seconds=10.0):
+    """Trains the step MLP on guiding centres drawn from the config-2
+    distributions (8,192 electrons, an independent draw from the benchmark's):
+    plain-controller samples then three on-policy rounds."""
+    from rapt_gb300 import learned, workloads as W
+    w = W.subsample(W.config2(), np.arange(0, 65536, 8))
+    t = time.perf_counter()
+    p, info = learned.fit_gc(w, seconds, ctx=ctx, rounds=3, steps=3000, capacity=1 << 23, mask=7)
+    info["seconds"] = time.perf_counter() - t
+    info["accepted_steps_generated"] = int(sum(c["accepted"] for c in info["collect"]))
+    return p, info
+
+
 def run_ours(args, rank, ws, dist):
     from rapt_gb300 import Ensemble, workloads as W, fields as F
     from rapt_gb300 import _native as N
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     ctx = N.Context(dev)
+    fp64_peak, fp32_peak = ctx.measure_peaks()
+    params, fit = train_step_model(ctx)
+    ctx.mlp_set_params(params)
     w = W.gc_bench(args.n, seed=rank)
     n = len(w["mass"])
     ens = Ensemble(F.DoubleDipole(), n, max_rows=4, ctx=ctx, pinned=not args.no_e2e)
     ens.configure(**w["params"])
     ens.set_guiding_centers(w["pos"], w["v"], pa=w["pa"], t0=0.0, mass=w["mass"], charge=w["charge"])
     init = {k: (v.copy()) for k, v in ens.h.items()}
-    ens.upload()
-    fp64_peak, fp32_peak = ctx.measure_peaks()
+    fgyro = gyro_frequency_sum(w, ens.field.magB(np.column_stack([np.zeros(n), w["pos"]])))
 
-    for _ in range(args.warmup):
-        ens.advance("gc", 1.0)
-        ens.rows(reset=True)
-    # ---- device-resident timed region
-    barrier(dist)
-    clk = Clocks(dev) if rank == 0 else None
-    t0 = time.perf_counter()
-    acc = 0
-    dev_ms = 0.0
-    launches = 0
-    for _ in range(args.steps):
-        st = ens.advance("gc", 1.0)
-        acc += st["accepted"]
-        dev_ms += st["kernel_ms"]
-        launches += st["kernel_launches"]
-        ens.ctx.check(ens.ctx.L.rapt_rows_download(ens.ctx.h, None, None, None, None, None, 1), "reset rows")
-    wall = time.perf_counter() - t0
-    clocks = clk.stop() if clk else None
-    barrier(dist)
-    dev_s = allmax(dist, dev_ms * 1e-3)
-    acc_all = allsum(dist, acc)
-    value = acc_all / dev_s
-    # ---- end to end through the public API with pinned host buffers
-    e2e = None
-    if not args.no_e2e:
+    def reset():
         for k, v in init.items():
             ens.h[k][...] = v
+        ens.upload()
+
+    results = {}
+    barrier(dist)
+    clk = Clocks(dev) if rank == 0 else None
+    t_all = time.perf_counter()
+    for name, form in FORMS:
+        reset()
+        ens.configure(form=form, learned_scale=fit["scale"], collect=0)
+        for _ in range(args.warmup):
+            ens.advance("gc", 1.0)
+            ens.rows(reset=True)
+        # ---- device-resident timed region
+        barrier(dist)
+        acc = rej = rhs = launches = 0
+        dev_ms = 0.0
+        for _ in range(args.steps):
+            st = ens.advance("gc", 1.0)
+            acc += st["accepted"]
+            rej += st["rejected"]
+            rhs += st["rhs_evals"]
+            dev_ms += st["kernel_ms"]
+            launches += st["kernel_launches"]
+            ens.ctx.check(ens.ctx.L.rapt_rows_download(ens.ctx.h, None, None, None, None, None, 1), "reset rows")
+        barrier(dist)
+        dev_s = allmax(dist, dev_ms * 1e-3)
+        acc_all = allsum(dist, acc)
+        sim = allsum(dist, float(n * args.steps))
+        results[name] = {"accepted_per_s": acc_all / dev_s, "ms_per_step": dev_s * 1e3 / args.steps,
+                         "accepted": int(acc), "rejected": int(rej), "rhs_evals": int(rhs),
+                         "reject_rate": rej / max(acc, 1), "rhs_per_tracer_second": rhs / (n * args.steps),
+                         "tracer_seconds_per_s": sim / dev_s,
+                         "gyro_periods_per_s": allsum(dist, fgyro * args.steps) / dev_s,
+                         "kernel_launches": int(launches), "device_ms": dev_ms}
+    wall = time.perf_counter() - t_all
+    clocks = clk.stop() if clk else None
+    head = results[HEADLINE]
+    plain = results["plain"]
+    for r in results.values():
+        r["accepted_per_s_vs_plain"] = r["accepted_per_s"] / plain["accepted_per_s"]
+        r["tracer_seconds_per_s_vs_plain"] = r["tracer_seconds_per_s"] / plain["tracer_seconds_per_s"]
+    # ---- end to end through the public API with pinned host buffers (headline form)
+    e2e = None
+    if not args.no_e2e:
+        reset()
+        ens.configure(form=dict(FORMS)[HEADLINE], learned_scale=fit["scale"])
         h2d = sum(ens.h[k].nbytes for k in ens.h)
         d2h = h2d + n * ens.max_rows * 8 * 8  # state back + rows buffer
         barrier(dist)
@@ -228,28 +281,38 @@ def run_ours(args, rank, ws, dist):
             ens.rows(reset=True)
         e2e_s = allmax(dist, time.perf_counter() - t1)
         e2e = {"value": allsum(dist, acc_e) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
+               "d2h_bytes_per_step": int(d2h), "form": HEADLINE}
     if rank != 0:
         return
-    achieved = FLOPS_PER_ACCEPTED_STEP * acc / (dev_ms * 1e-3) / 1e12
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+    achieved = FLOPS_PER_ACCEPTED_STEP * head["accepted"] / (head["device_ms"] * 1e-3) / 1e12
+    achieved_plain = FLOPS_PER_ACCEPTED_STEP * plain["accepted"] / (plain["device_ms"] * 1e-3) / 1e12
+    line = {"metric": METRIC, "value": head["accepted_per_s"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 stages (float-float) + f64 control/stencil",
             "data": "synthetic (seeded, config-2 distributions at 2^20 tracers per GPU)",
-            "config": {"workload": "gc_doubledipole_1M", "tracers_per_gpu": n, "form": "plain",
+            "config": {"workload": "gc_doubledipole_1M", "tracers_per_gpu": n, "form": HEADLINE,
                        "eom": "TaoChanBrizard", "method": "DOPRI5", "rtol": 1e-8, "atol": 1e-8,
                        "step": "GuidingCenter.advance(1.0) of every tracer",
                        "l2": "state 1M x 232 B > L2 (compute bound; no flush)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "forms": results,
+            "step_model": {"scale": fit["scale"], "train_seconds": fit["seconds"],
+                           "accepted_steps_generated": fit["accepted_steps_generated"],
+                           "samples": int(sum(c["samples"] for c in fit["collect"])),
+                           "calibration": fit["calibration"][-1], "losses": fit["losses"][-1]},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": achieved / fp64_peak, "traffic": None,
+                         "frac": achieved / fp64_peak, "traffic": None, "kernel": "k_gc32 (learned)",
                          "peak_source": "measured in-run: FP64 FMA chains (rapt_measure_peaks)",
-                         "flops_per_accepted_step": FLOPS_PER_ACCEPTED_STEP, "fp32_peak_tflops": fp32_peak},
-            "gpu_launches": int(launches), "clocks": clocks, "wall_s": wall}
+                         "flops_per_accepted_step": FLOPS_PER_ACCEPTED_STEP,
+                         "flops_note": "algorithmic FP64-equivalent flops of one DOPRI5 step",
+                         "plain_kernel": {"kernel": "k_gc", "achieved": achieved_plain,
+                                          "frac": achieved_plain / fp64_peak},
+                         "fp32_peak_tflops": fp32_peak},
+            "gpu_launches": int(head["kernel_launches"]), "clocks": clocks, "wall_s": wall}
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu_baseline:
-        n_s = args.cpu_sample or 4096
+        n_s = args.cpu_sample or 65536
         v, a, dt = cpu_baseline(n_s, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                 "sample": "%d of the 1,048,576 tracers, 1 s each (%.1f s)" % (n_s, dt)}

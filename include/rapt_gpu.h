@@ -97,6 +97,8 @@ typedef struct {
   int32_t use_graph;             /* 1: replay the launch sequence as a captured CUDA graph */
   int32_t collect;               /* 1: record step-size training samples (GC, DOPRI5; any form) */
   double learned_scale;          /* learned forms: multiplier on each MLP step proposal (0: 1) */
+  int32_t learned_every;         /* learned forms: run the MLP on every k-th accepted step and reuse its
+                                    correction in between (0 or 1: every step) */
 } rapt_config;
 
 /* Host-side SoA view of an ensemble. Any pointer may be NULL on download to

@@ -152,6 +152,7 @@ KParams make_params(const Ctx* c, int kind) {
   P.samp_cap = c->samp_cap;
   P.samp_mask = c->samp_mask;
   P.collect = g.collect;
+  P.learn_every = g.learned_every > 1 ? g.learned_every : 1;
   return P;
 }
 
@@ -299,6 +300,7 @@ int rapt_config_set(void* ctx, const rapt_config* g) {
   if ((g->form == RAPT_FORM_LEARNED || g->form == RAPT_FORM_LEARNED_FP32 || g->collect) && g->tableau != 0)
     return fail(c, RAPT_ERR_UNSUPPORTED, "the step learner drives the DOPRI5 controller (tableau 0)");
   if (!(g->learned_scale >= 0)) return fail(c, RAPT_ERR_INVALID, "learned_scale must be >= 0");
+  if (g->learned_every < 0) return fail(c, RAPT_ERR_INVALID, "learned_every must be >= 0");
   c->cfg = *g;
   return RAPT_OK;
 }

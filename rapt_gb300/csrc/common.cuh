@@ -47,6 +47,7 @@ struct KParams {
   long long samp_cap;
   unsigned long long samp_mask;  // an accepted step is sampled when its hash & mask == 0
   int collect;             // learned kernels: also record samples (on-policy data)
+  int learn_every;         // run the MLP on every k-th accepted step, reuse its correction between
 };
 
 // Device SoA ensemble (all arrays length n unless noted).

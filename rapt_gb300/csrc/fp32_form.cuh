@@ -35,6 +35,7 @@ __device__ __forceinline__ DF dff(double v) { return DF{(float)v, 0.f}; }
 // Generic: FP64 model evaluated at the float-float point, rounded to float-float.
 template <int M>
 struct FieldDF {
+  static constexpr bool kDF = false;  // evaluated in FP64 and rounded to float-float
   __device__ __forceinline__ static void B(const FieldP& f, double t, const DF* X, DF* o) {
     double b[3];
     Field<M>::B(f, t, df_to_double(X[0]), df_to_double(X[1]), df_to_double(X[2]), b);
@@ -51,6 +52,7 @@ __device__ __forceinline__ DF inv_re() { return DF(DFc(1.0 / kRe)); }
 
 template <>
 struct FieldDF<RAPT_EARTH_DIPOLE> {
+  static constexpr bool kDF = true;
   // B = -3 B0 (rx rz, ry rz, rz^2 - r^2/3) / r^5 with r = x / Re
   __device__ __forceinline__ static void B(const FieldP& f, double, const DF* X, DF* o) {
     const DF x = X[0] * inv_re(), y = X[1] * inv_re(), z = X[2] * inv_re();
@@ -69,6 +71,7 @@ struct FieldDF<RAPT_EARTH_DIPOLE> {
 
 template <>
 struct FieldDF<RAPT_DOUBLE_DIPOLE> {
+  static constexpr bool kDF = true;
   __device__ __forceinline__ static void B(const FieldP& f, double, const DF* X, DF* o) {
     const DF x = X[0] * inv_re(), y = X[1] * inv_re(), z = X[2] * inv_re();
     const DF yz2 = y * y + z * z;
@@ -85,6 +88,38 @@ struct FieldDF<RAPT_DOUBLE_DIPOLE> {
     o[0] = o[1] = o[2] = DF{0.f, 0.f};
   }
 };
+
+// grad|B| and curl b by the reference's central differences (fields.py:155-200,
+// the 6-point stencil of stencil_gradB_curlb): the six field samples, their
+// magnitudes and unit vectors in float-float (about 48 bits), the differences
+// of the samples in float-float (exact for these nearby values), and the
+// difference quotients in FP64. The samples' rounding adds about 1e-10
+// relative to the gradients, far below the stencil's own truncation error
+// ((gradstep / r)^2, about 4e-8 at 5 Re).
+template <int M>
+__device__ __forceinline__ void stencil_gradB_curlb_df(const FieldP& f, double t, const DF* Y, double* gB,
+                                                       double* cb) {
+  const DF d = dfd(f.gradstep);
+  double c0 = 0.0, c1 = 0.0, c2 = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    DF xp[3] = {Y[0], Y[1], Y[2]}, xm[3] = {Y[0], Y[1], Y[2]};
+    xp[a] = Y[a] + d;
+    xm[a] = Y[a] - d;
+    DF bp[3], bm[3];
+    FieldDF<M>::B(f, t, xp, bp);
+    FieldDF<M>::B(f, t, xm, bm);
+    const DF sp = bp[0] * bp[0] + bp[1] * bp[1] + bp[2] * bp[2];
+    const DF sm = bm[0] * bm[0] + bm[1] * bm[1] + bm[2] * bm[2];
+    const DF ip = df_rsqrt(sp), im = df_rsqrt(sm);
+    gB[a] = df_to_double(sp * ip - sm * im) * f.inv2d;
+    auto du = [&](int i) { return df_to_double(bp[i] * ip - bm[i] * im); };
+    if (a == 0) { c1 -= du(2); c2 += du(1); }
+    if (a == 1) { c0 += du(2); c2 -= du(0); }
+    if (a == 2) { c0 -= du(1); c1 += du(0); }
+  }
+  cb[0] = c0 * f.inv2d; cb[1] = c1 * f.inv2d; cb[2] = c2 * f.inv2d;
+}
 
 // ---------------------------------------------------------------- right-hand sides
 // Particle, Y = (x, y, z [m], ux, uy, uz [p/(m c)]):
@@ -126,10 +161,16 @@ struct GcRHSdf {
     const DF ib = df_rsqrt(b2);
     const DF Bmag = b2 * ib;
     const DF ub[3] = {B[0] * ib, B[1] * ib, B[2] * ib};
-    const double Xd[3] = {df_to_double(Y[0]), df_to_double(Y[1]), df_to_double(Y[2])};
     double gBd[3], cbd[3], dbd[3];
-    stencil_gradB_curlb<M>(f, t, Xd, gBd, cbd);
-    dbdt<M>(f, t, Xd, dbd);
+    if constexpr (FieldDF<M>::kDF) {
+      stencil_gradB_curlb_df<M>(f, t, Y, gBd, cbd);
+      dbd[0] = dbd[1] = dbd[2] = 0.0;
+      static_assert(!FieldDF<M>::kDF || Field<M>::kStatic, "float-float field models are static");
+    } else {
+      const double Xd[3] = {df_to_double(Y[0]), df_to_double(Y[1]), df_to_double(Y[2])};
+      stencil_gradB_curlb<M>(f, t, Xd, gBd, cbd);
+      dbdt<M>(f, t, Xd, dbd);
+    }
     DF E[3];
     FieldDF<M>::E(f, t, Y, E);
     const DF rg = df_rsqrt(DF{1.f, 0.f} + kmu * Bmag + u * u);
@@ -190,6 +231,64 @@ __device__ __forceinline__ void dopri5_attempt_df(const F& f, double x, const DF
     y1[i] = y[i] + hd * (k1[i] * DF(DFc(a71)) + k3[i] * DF(DFc(a73)) + k4[i] * DF(DFc(a74)) +
                          k5[i] * DF(DFc(a75)) + k6[i] * DF(DFc(a76)));
   f(xph, y1, k7);
+  double e = 0.0;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const DF ei = k1[i] * DF(DFc(e1)) + k3[i] * DF(DFc(e3)) + k4[i] * DF(DFc(e4)) + k5[i] * DF(DFc(e5)) +
+                  k6[i] * DF(DFc(e6)) + k7[i] * DF(DFc(e7));
+    const double r = df_to_double(ei) * h * scale[i] / err_sk(y[i], y1[i], scale[i], rtol, atol);
+    e += r * r;
+  }
+  err = sqrt(e * (1.0 / NV));
+}
+
+// The DOPRI5 tableau as float-float pairs in constant memory (rows as kDp5A).
+struct DFpair {
+  float hi, lo;
+};
+constexpr DFpair dfp(double v) { return DFpair{(float)v, (float)(v - (double)(float)v)}; }
+static __constant__ DFpair kDp5Adf[7][6] = {
+    {dfp(0), dfp(0), dfp(0), dfp(0), dfp(0), dfp(0)},
+    {dfp(dp5::a21), dfp(0), dfp(0), dfp(0), dfp(0), dfp(0)},
+    {dfp(dp5::a31), dfp(dp5::a32), dfp(0), dfp(0), dfp(0), dfp(0)},
+    {dfp(dp5::a41), dfp(dp5::a42), dfp(dp5::a43), dfp(0), dfp(0), dfp(0)},
+    {dfp(dp5::a51), dfp(dp5::a52), dfp(dp5::a53), dfp(dp5::a54), dfp(0), dfp(0)},
+    {dfp(dp5::a61), dfp(dp5::a62), dfp(dp5::a63), dfp(dp5::a64), dfp(dp5::a65), dfp(0)},
+    {dfp(dp5::a71), dfp(0), dfp(dp5::a73), dfp(dp5::a74), dfp(dp5::a75), dfp(dp5::a76)}};
+
+// The same DOPRI5 attempt with the six right-hand sides in one rolled loop:
+// the right-hand side (float-float field, stencil and equations) is emitted
+// once instead of six times, which keeps the kernel inside the instruction
+// cache at the high occupancy this form runs at. The zero coefficients add
+// exact zeros, so the results equal dopri5_attempt_df's.
+template <int NV, class F>
+__device__ __forceinline__ void dopri5_attempt_df_rolled(const F& f, double x, const DF* y, const DF* k1, double h,
+                                                         const double* scale, double rtol, double atol, DF* y1,
+                                                         DF* k7, double& err) {
+  using namespace dp5;
+  const DF hd = dfd(h);
+  DF k2[NV], k3[NV], k4[NV], k5[NV], k6[NV], yt[NV], kt[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) k2[i] = k3[i] = k4[i] = k5[i] = k6[i] = DF{0.f, 0.f};
+#pragma unroll 1
+  for (int s = 1; s <= 6; ++s) {
+    const DFpair* A = kDp5Adf[s];
+    const DF a0{A[0].hi, A[0].lo}, a1{A[1].hi, A[1].lo}, a2{A[2].hi, A[2].lo}, a3{A[3].hi, A[3].lo},
+        a4{A[4].hi, A[4].lo}, a5{A[5].hi, A[5].lo};
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+      yt[i] = y[i] + hd * (k1[i] * a0 + k2[i] * a1 + k3[i] * a2 + k4[i] * a3 + k5[i] * a4 + k6[i] * a5);
+    f(x + kDp5C[s] * h, yt, kt);
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      if (s == 1) k2[i] = kt[i];
+      if (s == 2) k3[i] = kt[i];
+      if (s == 3) k4[i] = kt[i];
+      if (s == 4) k5[i] = kt[i];
+      if (s == 5) k6[i] = kt[i];
+      if (s == 6) { k7[i] = kt[i]; y1[i] = yt[i]; }
+    }
+  }
   double e = 0.0;
 #pragma unroll
   for (int i = 0; i < NV; ++i) {

@@ -10,7 +10,8 @@
 namespace rapt {
 
 template <int M>
-__global__ void __launch_bounds__(128) k_particle32(DevEnsemble E, KParams P, Scratch* S) {
+// 4 blocks per SM: measured best for the 12-stage DOP853 float-float kernel.
+__global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P, Scratch* S) {
   int64_t idx = -1;
   bool exhausted = false;
   long long budget = P.budget;
@@ -233,13 +234,18 @@ __global__ void __launch_bounds__(128) k_particle32(DevEnsemble E, KParams P, Sc
 
 template <int M, int LRN = 0>
 // LRN: 0 plain controller, 1 training-sample collection, 2 MLP step proposals.
-__global__ void __launch_bounds__(128) k_gc32(DevEnsemble E, KParams P, Scratch* S) {
+// 16 blocks of 128 threads per SM (32 registers, the rest spilled to L1/L2):
+// the float-float stages are long dependent FP32 chains, and on GB300 more
+// resident warps hide their latency better than registers avoid the spills
+// (measured at 262k tracers: 1.11e8 accepted steps/s at 1 block/SM, 1.93e8 at
+// 8, 2.37e8 at 16).
+__global__ void __launch_bounds__(128, 16) k_gc32(DevEnsemble E, KParams P, Scratch* S) {
   int64_t idx = -1;
   bool exhausted = false;
   long long budget = P.budget;
   LaneStats st;
   StepLearner<LRN> lr;
-  lr.init();
+  lr.init(P);
   double errold = 1e-4;  // previous accepted error (learner feature)
 
   DF y[4];
@@ -378,7 +384,7 @@ __global__ void __launch_bounds__(128) k_gc32(DevEnsemble E, KParams P, Scratch*
       --budget;
       DF y1[4], k7[4];
       double err;
-      dopri5_attempt_df<4>(rhs, rt, y, k1, h, scale, P.rtol, P.atol, y1, k7, err);
+      dopri5_attempt_df_rolled<4>(rhs, rt, y, k1, h, scale, P.rtol, P.atol, y1, k7, err);
       nfcn += 6;
       st.rhs += 6;
       lr.on_attempt(P, h, err, last);

@@ -52,30 +52,32 @@ int occ_gc32(int block) {
   return nb;
 }
 // guiding-centre kernels with the step learner; dynamic shared memory per warp
+// (the occupancy is taken without collection; a collecting launch needs more
+// shared memory per block, and its surplus blocks start as others finish)
 template <int LRN>
-size_t lrn_smem(int block) {
-  return (size_t)(block / 32) * StepLearner<LRN>::kWarpWords * sizeof(uint32_t);
+size_t lrn_smem(int block, bool collect) {
+  return (size_t)(block / 32) * StepLearner<LRN>::warp_words(collect) * sizeof(uint32_t);
 }
 template <int LRN>
 cudaError_t launch_gc_lrn(const LaunchArgs& a) {
-  k_gc<kM, 0, LRN><<<a.grid, a.block, lrn_smem<LRN>(a.block), a.stream>>>(a.E, a.P, a.S);
+  k_gc<kM, 0, LRN><<<a.grid, a.block, lrn_smem<LRN>(a.block, a.P.collect != 0), a.stream>>>(a.E, a.P, a.S);
   return cudaGetLastError();
 }
 template <int LRN>
 cudaError_t launch_gc32_lrn(const LaunchArgs& a) {
-  k_gc32<kM, LRN><<<a.grid, a.block, lrn_smem<LRN>(a.block), a.stream>>>(a.E, a.P, a.S);
+  k_gc32<kM, LRN><<<a.grid, a.block, lrn_smem<LRN>(a.block, a.P.collect != 0), a.stream>>>(a.E, a.P, a.S);
   return cudaGetLastError();
 }
 template <int LRN>
 int occ_gc_lrn(int block) {
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc<kM, 0, LRN>, block, lrn_smem<LRN>(block));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc<kM, 0, LRN>, block, lrn_smem<LRN>(block, false));
   return nb;
 }
 template <int LRN>
 int occ_gc32_lrn(int block) {
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc32<kM, LRN>, block, lrn_smem<LRN>(block));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc32<kM, LRN>, block, lrn_smem<LRN>(block, false));
   return nb;
 }
 cudaError_t field_eval(const FieldP& f, int what, int64_t n, const double* tpos, double* out, cudaStream_t s) {

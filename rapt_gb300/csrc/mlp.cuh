@@ -145,26 +145,86 @@ __device__ __forceinline__ void stage_features(const float* p, const float* f, u
   }
 }
 
-// Per-warp shared memory of inference (u32): X [32][8], H1 [32][32], H2 [32][32].
-constexpr int kWarpSmemInfer = 32 * 8 + 32 * 32 + 32 * 32;
+// Two ReLU-layer C fragments (n-tiles 2s, 2s+1 of a 16-row tile) packed as the
+// BF16 A fragment of the next layer's k-step s: a0 = tile 2s rows g, a1 = tile
+// 2s rows g+8, a2/a3 = tile 2s+1 (the C and A layouts of m16n8k16 line up).
+__device__ __forceinline__ void relu_pack_a(const float* c0, const float* c1, uint32_t* a) {
+  a[0] = pack_bf16x2(fmaxf(c0[0], 0.f), fmaxf(c0[1], 0.f));
+  a[1] = pack_bf16x2(fmaxf(c0[2], 0.f), fmaxf(c0[3], 0.f));
+  a[2] = pack_bf16x2(fmaxf(c1[0], 0.f), fmaxf(c1[1], 0.f));
+  a[3] = pack_bf16x2(fmaxf(c1[2], 0.f), fmaxf(c1[3], 0.f));
+}
 
-// Whole-warp inference on the staged X rows; every lane gets its row's two
-// outputs in target units. All 32 lanes must call it (mma.sync).
-__device__ __forceinline__ void mlp_forward_staged(const uint32_t* w, const float* p, uint32_t* sm, float* out) {
+// Per-warp shared memory of inference (u32): the staged inputs X [32][8].
+constexpr int kWarpSmemInfer = 32 * 8;
+
+// Whole-warp inference on the staged X rows, one 16-row tile at a time, with
+// the hidden activations kept in registers as A fragments (H1) or consumed
+// as soon as a pair of n-tiles is complete (H2); the BF16 roundings are those
+// of storing H1 and H2. Every lane gets its row's two outputs in target units.
+// All 32 lanes must call it (mma.sync).
+__device__ __forceinline__ void mlp_forward_staged(const uint32_t* w, const float* p, const uint32_t* X,
+                                                   float* out) {
   const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
-  uint32_t* X = sm;
-  uint32_t* H1 = X + 32 * 8;
-  uint32_t* H2 = H1 + 32 * 32;
+  const uint32_t *W1T = w + kPW1, *W2T = w + kPW2, *W3T = w + kPW3;
+  const float *b1 = p + kOffB1, *b2 = p + kOffB2, *b3 = p + kOffB3;
   __syncwarp();
-  dense_relu<16, 64>(X, w + kPW1, p + kOffB1, H1, g, q);
+  float c3[2][4];
+#pragma unroll
+  for (int t = 0; t < 2; ++t) {
+    uint32_t xa[4];
+    load_a(X, 8, t, 0, g, q, xa);
+    uint32_t h1[4][4];  // layer-2 A fragments, k-steps 0..3
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      float c[2][4];
+#pragma unroll
+      for (int jj = 0; jj < 2; ++jj) {
+        const int j = 2 * s + jj;
+        c[jj][0] = c[jj][2] = b1[8 * j + 2 * q];
+        c[jj][1] = c[jj][3] = b1[8 * j + 2 * q + 1];
+        uint32_t b[2];
+        load_b(W1T, 8, j, 0, g, q, b);
+        mma_bf16(c[jj], xa, b);
+      }
+      relu_pack_a(c[0], c[1], h1[s]);
+    }
+    c3[t][0] = c3[t][2] = b3[2 * q];
+    c3[t][1] = c3[t][3] = b3[2 * q + 1];
+#pragma unroll
+    for (int s3 = 0; s3 < 4; ++s3) {
+      float c2[2][4];
+#pragma unroll
+      for (int jj = 0; jj < 2; ++jj) {
+        const int j = 2 * s3 + jj;
+        c2[jj][0] = c2[jj][2] = b2[8 * j + 2 * q];
+        c2[jj][1] = c2[jj][3] = b2[8 * j + 2 * q + 1];
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          uint32_t b[2];
+          load_b(W2T, 32, j, s, g, q, b);
+          mma_bf16(c2[jj], h1[s], b);
+        }
+      }
+      uint32_t a3[4], bw[2];
+      relu_pack_a(c2[0], c2[1], a3);
+      load_b(W3T, 32, 0, s3, g, q, bw);
+      mma_bf16(c3[t], a3, bw);
+    }
+  }
   __syncwarp();
-  dense_relu<64, 64>(H1, w + kPW2, p + kOffB2, H2, g, q);
-  __syncwarp();
-  float y[2];
-  dense_out(H2, w + kPW3, p + kOffB3, g, q, lane, y);
-  __syncwarp();
-  out[0] = y[0] * p[kOffYsig] + p[kOffYmu];
-  out[1] = y[1] * p[kOffYsig + 1] + p[kOffYmu + 1];
+  // sample 16 t + rr sits on lane 4 (rr % 8), columns 0..1, in c3[t][0..1] (rr < 8) or c3[t][2..3]
+  const int rr = lane & 15, src = 4 * (rr & 7);
+  float v[2][4];
+#pragma unroll
+  for (int tt = 0; tt < 2; ++tt)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[tt][i] = __shfl_sync(kFull, c3[tt][i], src);
+  const bool hi_t = lane >= 16, hi_r = rr >= 8;
+  const float y0 = hi_t ? (hi_r ? v[1][2] : v[1][0]) : (hi_r ? v[0][2] : v[0][0]);
+  const float y1 = hi_t ? (hi_r ? v[1][3] : v[1][1]) : (hi_r ? v[0][3] : v[0][1]);
+  out[0] = y0 * p[kOffYsig] + p[kOffYmu];
+  out[1] = y1 * p[kOffYsig + 1] + p[kOffYmu + 1];
 }
 
 __host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
@@ -188,21 +248,30 @@ struct StepLearner {
   // shared memory per warp: inference buffers (LRN 2), then raw feature rows of
   // the samples being collected
   static constexpr int kRawOff = LRN == 2 ? kWarpSmemInfer : 0;
-  static constexpr int kWarpWords = LRN == 0 ? 0 : kRawOff + 32 * 16;
+  // words per warp of a launch: the raw rows only when samples are collected
+  __host__ __device__ static constexpr int warp_words(bool collect) {
+    return LRN == 0 ? 0 : kRawOff + ((LRN == 1 || collect) ? 32 * 16 : 0);
+  }
   float c_mass, c_energy, c_sign, c_pitch;  // per-tracer feature constants
   float rcap;                               // cap on the learned correction
+  float rlast;                              // last correction of the network (reused between calls)
+  int since;                                // accepted steps since the last network call
   double hbase;                             // collect: the controller's step after the sampled step
   double hcont;                             // learned: the step wanted before the interval-end clip
   bool want, pend, have_prop;
   uint32_t* sm;
 
-  __device__ __forceinline__ void init() {
+  __device__ __forceinline__ void init(const KParams& P) {
     want = pend = have_prop = false;
-    sm = LRN ? rapt_dyn_smem + (threadIdx.x >> 5) * kWarpWords : nullptr;
+    rlast = 1.f;
+    since = 0;
+    sm = LRN ? rapt_dyn_smem + (threadIdx.x >> 5) * warp_words(P.collect != 0) : nullptr;
   }
   // Per-tracer constants; vs is the speed, pitch scale converts ppar to cos(pitch).
   __device__ __forceinline__ void load(double mass, double charge, double vs, double ppar_unit) {
     want = pend = have_prop = false;
+    rlast = 1.f;
+    since = 0;
     if constexpr (LRN != 0) {
       const double gam = 1.0 / sqrt(1.0 - (vs / kC) * (vs / kC));
       c_mass = log10f((float)(mass / kMe));
@@ -235,7 +304,16 @@ struct StepLearner {
     }
     const bool coll = (LRN == 1 || P.collect) &&
                       (mix64((uint64_t)idx * 0x100000001b3ull + (uint64_t)nacc) & P.samp_mask) == 0;
-    const bool inf = LRN == 2 && allow;
+    bool inf = LRN == 2 && allow;
+    if constexpr (LRN == 2) {
+      if (inf && P.learn_every > 1 && ++since < P.learn_every) {
+        // between network calls: the last correction on the controller's step
+        float cap = (float)(hmax / fabs(hnew));
+        if (rej_before) cap = fminf(cap, (float)(fabs(h) / fabs(hnew)));
+        hnew *= (double)fminf(rlast, cap);
+        inf = false;
+      }
+    }
     if (!coll && !inf) return;
     float f[16];
     const float r = sqrtf(x * x + y * y + z * z);
@@ -299,8 +377,10 @@ struct StepLearner {
         float o[2];
         mlp_forward_staged(P.mlp_w, P.mlp_p, sm, o);
         if (want) {
-          const float r = fminf(__expf(fminf(fmaxf(o[0], -3.f), 3.f)) * P.learn_scale, rcap);
-          h *= (double)r;
+          const float rn = __expf(fminf(fmaxf(o[0], -3.f), 3.f)) * P.learn_scale;
+          rlast = rn;
+          since = 0;
+          h *= (double)fminf(rn, rcap);
         }
       }
       want = false;

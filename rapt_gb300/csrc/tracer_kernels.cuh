@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
   long long budget = P.budget;
   LaneStats st;
   StepLearner<LRN> lr;
-  lr.init();
+  lr.init(P);
 
   double y[4] = {0, 0, 0, 0}, k1[4] = {0, 0, 0, 0};
   double rt = 0, t_row = 0, tcur = 0, dt = 0, stop = 0, mass = 0, charge = 0, delta = 0, mu = 0, vs = 0;

@@ -150,6 +150,8 @@ def fit_gc(workload, seconds, ctx=None, rounds=2, steps=3000, batch=4096, lr=2e-
     info["calibration"].append(cal)
     for r in range(rounds):
         n0, n1 = run(2, cal["scale"])
+        if n1 == n0:
+            raise RuntimeError("sample buffer full: raise capacity or mask")
         p, losses = train(ctx, steps, batch, lr, seed + 10 * (r + 1), params=p)
         info["losses"].append(losses)
         cal = calibrate(ctx, ctx.mlp_samples_download(n0, min(n1 - n0, 1 << 16)))
