@@ -38,7 +38,8 @@ struct ModelTable {
 };
 
 // MLP kernels (mlp.cu); packed BF16 weights take kMlpPackedWords u32
-constexpr int kMlpPackedWords = 64 * 8 + 64 * 32 + 8 * 32 + 64 * 32 + 64 * 4;
+constexpr int kMlpPackedWords = 64 * 8 + 64 * 32 + 8 * 32 + 64 * 32 + 64 * 4 + 8 * 32 * 2 + 8 * 32 * 8 + 32 * 8 +
+                                 32 * 16 + 32 * 16 + 32 * 2;
 cudaError_t mlp_pack(const float* p, uint32_t* w, cudaStream_t s);
 cudaError_t mlp_grad(const float* samples, int64_t nsamp, int64_t batch, int random, uint64_t seed, int64_t step,
                      float switch_weight, const uint32_t* w, const float* p, float* grad, double* loss, int num_sms,

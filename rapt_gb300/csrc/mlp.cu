@@ -264,9 +264,31 @@ __global__ void k_mlp_pack(const float* p, uint32_t* w) {
   } else if (s < kPW3N) {
     const int r = s - kPW2N, in = r / 32, o2 = r % 32;
     lo = p[kOffW2 + (2 * o2) * 64 + in]; hi = p[kOffW2 + (2 * o2 + 1) * 64 + in];
-  } else {
+  } else if (s < kPF1) {
     const int r = s - kPW3N, in = r / 4, o2 = r % 4;
     lo = p[kOffW3 + (2 * o2) * 64 + in]; hi = p[kOffW3 + (2 * o2 + 1) * 64 + in];
+  } else if (s < kPB1) {
+    // B fragments of one lane (g = lane / 4, q = lane % 4): u32 column c of W?T row n
+    int row, c, base, stride;
+    if (s < kPF2) {         // W1: [j][lane][k], k-step 0
+      const int r = s - kPF1, j = r / 64, lane = (r / 2) % 32, k = r % 2;
+      row = 8 * j + lane / 4; c = lane % 4 + 4 * k; base = kOffW1; stride = 16;
+    } else if (s < kPF3) {  // W2: [j][lane][2 s + half]
+      const int r = s - kPF2, j = r / 256, lane = (r / 8) % 32, k = r % 8;
+      row = 8 * j + lane / 4; c = 8 * (k / 2) + lane % 4 + 4 * (k % 2); base = kOffW2; stride = 64;
+    } else {                // W3: [lane][2 s3 + half], n-tile 0
+      const int r = s - kPF3, lane = r / 8, k = r % 8;
+      row = lane / 4; c = 8 * (k / 2) + lane % 4 + 4 * (k % 2); base = kOffW3; stride = 64;
+    }
+    lo = p[base + row * stride + 2 * c]; hi = p[base + row * stride + 2 * c + 1];
+  } else {
+    // bias pairs of one lane, stored as float bits
+    int idx;
+    if (s < kPB2) { const int r = s - kPB1, lane = r / 16, k = r % 16; idx = kOffB1 + 8 * (k / 2) + 2 * (lane % 4) + k % 2; }
+    else if (s < kPB3) { const int r = s - kPB2, lane = r / 16, k = r % 16; idx = kOffB2 + 8 * (k / 2) + 2 * (lane % 4) + k % 2; }
+    else { const int r = s - kPB3, lane = r / 2, k = r % 2; idx = kOffB3 + 2 * (lane % 4) + k; }
+    w[s] = __float_as_uint(p[idx]);
+    return;
   }
   w[s] = pack_bf16x2(lo, hi);
 }

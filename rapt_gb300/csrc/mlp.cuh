@@ -41,7 +41,15 @@ constexpr int kPW2 = kPW1 + 64 * 8;            // W2T [64][32]
 constexpr int kPW3 = kPW2 + 64 * 32;           // W3T [8][32]
 constexpr int kPW2N = kPW3 + 8 * 32;           // W2  [64 in][32]: B operand of the backward pass
 constexpr int kPW3N = kPW2N + 64 * 32;         // W3  [64 in][4]
-constexpr int kMlpPacked = kPW3N + 64 * 4;
+// inference fragments: each lane's mma B fragments and bias pairs stored
+// contiguously, so that one call loads them with a few vector loads
+constexpr int kPF1 = kPW3N + 64 * 4;           // W1: [8 n-tiles][32 lanes][2]
+constexpr int kPF2 = kPF1 + 8 * 32 * 2;        // W2: [8 n-tiles][32 lanes][8] (4 k-steps x 2)
+constexpr int kPF3 = kPF2 + 8 * 32 * 8;        // W3: [32 lanes][8] (4 k-steps x 2)
+constexpr int kPB1 = kPF3 + 32 * 8;            // b1: [32 lanes][16] (8 n-tiles x 2), float bits
+constexpr int kPB2 = kPB1 + 32 * 16;           // b2: [32 lanes][16]
+constexpr int kPB3 = kPB2 + 32 * 16;           // b3: [32 lanes][2]
+constexpr int kMlpPacked = kPB3 + 32 * 2;
 
 extern __shared__ __align__(16) uint32_t rapt_dyn_smem[];
 
@@ -161,13 +169,18 @@ constexpr int kWarpSmemInfer = 32 * 8;
 // Whole-warp inference on the staged X rows, one 16-row tile at a time, with
 // the hidden activations kept in registers as A fragments (H1) or consumed
 // as soon as a pair of n-tiles is complete (H2); the BF16 roundings are those
-// of storing H1 and H2. Every lane gets its row's two outputs in target units.
-// All 32 lanes must call it (mma.sync).
-__device__ __forceinline__ void mlp_forward_staged(const uint32_t* w, const float* p, const uint32_t* X,
-                                                   float* out) {
+// of storing H1 and H2. Weights and biases come from the per-lane fragment
+// layout (kPF*, kPB*) in vector loads. Every lane gets its row's two outputs
+// in target units. All 32 lanes must call it (mma.sync).
+__device__ __forceinline__ void mlp_forward_staged(const uint32_t* __restrict__ w, const float* __restrict__ p,
+                                                   const uint32_t* X, float* out) {
   const int lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
-  const uint32_t *W1T = w + kPW1, *W2T = w + kPW2, *W3T = w + kPW3;
-  const float *b1 = p + kOffB1, *b2 = p + kOffB2, *b3 = p + kOffB3;
+  const uint2* F1 = reinterpret_cast<const uint2*>(w + kPF1) + lane;          // + 32 j
+  const uint4* F2 = reinterpret_cast<const uint4*>(w + kPF2) + 2 * lane;      // + 64 j
+  const uint4* F3 = reinterpret_cast<const uint4*>(w + kPF3) + 2 * lane;
+  const float4* B1 = reinterpret_cast<const float4*>(w + kPB1) + 4 * lane;
+  const float4* B2 = reinterpret_cast<const float4*>(w + kPB2) + 4 * lane;
+  const float2 b3 = __ldg(reinterpret_cast<const float2*>(w + kPB3) + lane);
   __syncwarp();
   float c3[2][4];
 #pragma unroll
@@ -177,38 +190,34 @@ __device__ __forceinline__ void mlp_forward_staged(const uint32_t* w, const floa
     uint32_t h1[4][4];  // layer-2 A fragments, k-steps 0..3
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-      float c[2][4];
+      const float4 bb = __ldg(B1 + s);  // biases of n-tiles 2s, 2s+1
+      float c[2][4] = {{bb.x, bb.y, bb.x, bb.y}, {bb.z, bb.w, bb.z, bb.w}};
 #pragma unroll
       for (int jj = 0; jj < 2; ++jj) {
-        const int j = 2 * s + jj;
-        c[jj][0] = c[jj][2] = b1[8 * j + 2 * q];
-        c[jj][1] = c[jj][3] = b1[8 * j + 2 * q + 1];
-        uint32_t b[2];
-        load_b(W1T, 8, j, 0, g, q, b);
+        const uint2 bf = __ldg(F1 + 32 * (2 * s + jj));
+        const uint32_t b[2] = {bf.x, bf.y};
         mma_bf16(c[jj], xa, b);
       }
       relu_pack_a(c[0], c[1], h1[s]);
     }
-    c3[t][0] = c3[t][2] = b3[2 * q];
-    c3[t][1] = c3[t][3] = b3[2 * q + 1];
+    c3[t][0] = c3[t][2] = b3.x;
+    c3[t][1] = c3[t][3] = b3.y;
 #pragma unroll
     for (int s3 = 0; s3 < 4; ++s3) {
-      float c2[2][4];
+      const float4 bb = __ldg(B2 + s3);
+      float c2[2][4] = {{bb.x, bb.y, bb.x, bb.y}, {bb.z, bb.w, bb.z, bb.w}};
 #pragma unroll
       for (int jj = 0; jj < 2; ++jj) {
         const int j = 2 * s3 + jj;
-        c2[jj][0] = c2[jj][2] = b2[8 * j + 2 * q];
-        c2[jj][1] = c2[jj][3] = b2[8 * j + 2 * q + 1];
+        const uint4 f0 = __ldg(F2 + 64 * j), f1 = __ldg(F2 + 64 * j + 1);
+        const uint32_t bk[4][2] = {{f0.x, f0.y}, {f0.z, f0.w}, {f1.x, f1.y}, {f1.z, f1.w}};
 #pragma unroll
-        for (int s = 0; s < 4; ++s) {
-          uint32_t b[2];
-          load_b(W2T, 32, j, s, g, q, b);
-          mma_bf16(c2[jj], h1[s], b);
-        }
+        for (int s = 0; s < 4; ++s) mma_bf16(c2[jj], h1[s], bk[s]);
       }
-      uint32_t a3[4], bw[2];
+      const uint4 f3 = __ldg(F3 + (s3 >> 1));
+      const uint32_t bw[2] = {(s3 & 1) ? f3.z : f3.x, (s3 & 1) ? f3.w : f3.y};
+      uint32_t a3[4];
       relu_pack_a(c2[0], c2[1], a3);
-      load_b(W3T, 32, 0, s3, g, q, bw);
       mma_bf16(c3[t], a3, bw);
     }
   }
