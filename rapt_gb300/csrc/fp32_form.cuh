@@ -96,6 +96,20 @@ struct FieldDF<RAPT_DOUBLE_DIPOLE> {
 // difference quotients in FP64. The samples' rounding adds about 1e-10
 // relative to the gradients, far below the stencil's own truncation error
 // ((gradstep / r)^2, about 4e-8 at 5 Re).
+// One stencil sample: |B| and B at x, float-float. Not inlined, so that the
+// kernel holds one copy of the field code for all six samples (the kernel runs
+// at high occupancy and its instruction cache is the limit).
+template <int M>
+__device__ __noinline__ void stencil_sample_df(const FieldP& f, double t, DF x0, DF x1, DF x2, DF* mag, DF* u) {
+  const DF x[3] = {x0, x1, x2};
+  DF b[3];
+  FieldDF<M>::B(f, t, x, b);
+  const DF s2 = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+  const DF ib = df_rsqrt(s2);
+  *mag = s2 * ib;
+  u[0] = b[0] * ib; u[1] = b[1] * ib; u[2] = b[2] * ib;
+}
+
 template <int M>
 __device__ __forceinline__ void stencil_gradB_curlb_df(const FieldP& f, double t, const DF* Y, double* gB,
                                                        double* cb) {
@@ -106,14 +120,11 @@ __device__ __forceinline__ void stencil_gradB_curlb_df(const FieldP& f, double t
     DF xp[3] = {Y[0], Y[1], Y[2]}, xm[3] = {Y[0], Y[1], Y[2]};
     xp[a] = Y[a] + d;
     xm[a] = Y[a] - d;
-    DF bp[3], bm[3];
-    FieldDF<M>::B(f, t, xp, bp);
-    FieldDF<M>::B(f, t, xm, bm);
-    const DF sp = bp[0] * bp[0] + bp[1] * bp[1] + bp[2] * bp[2];
-    const DF sm = bm[0] * bm[0] + bm[1] * bm[1] + bm[2] * bm[2];
-    const DF ip = df_rsqrt(sp), im = df_rsqrt(sm);
-    gB[a] = df_to_double(sp * ip - sm * im) * f.inv2d;
-    auto du = [&](int i) { return df_to_double(bp[i] * ip - bm[i] * im); };
+    DF mp, mm, up[3], um[3];
+    stencil_sample_df<M>(f, t, xp[0], xp[1], xp[2], &mp, up);
+    stencil_sample_df<M>(f, t, xm[0], xm[1], xm[2], &mm, um);
+    gB[a] = df_to_double(mp - mm) * f.inv2d;
+    auto du = [&](int i) { return df_to_double(up[i] - um[i]); };
     if (a == 0) { c1 -= du(2); c2 += du(1); }
     if (a == 1) { c0 += du(2); c2 -= du(0); }
     if (a == 2) { c0 -= du(1); c1 += du(0); }
@@ -153,7 +164,8 @@ struct GcRHSdf {
   FieldP f;
   DF kmu, mcq, muq, qmc;  // 2 mu/(m c^2), m c/q, mu/q, q/(m c)
   bool eq;
-  __device__ __forceinline__ void operator()(double t, const DF* Y, DF* o) const {
+  // not inlined: one copy serves HINIT, the first slope and the rolled stages
+  __device__ __noinline__ void operator()(double t, const DF* Y, DF* o) const {
     const DF u = Y[3];
     DF B[3];
     FieldDF<M>::B(f, t, Y, B);

@@ -182,9 +182,14 @@ __device__ __forceinline__ void mlp_forward_staged(const uint32_t* __restrict__ 
   const float4* B2 = reinterpret_cast<const float4*>(w + kPB2) + 4 * lane;
   const float2 b3 = __ldg(reinterpret_cast<const float2*>(w + kPB3) + lane);
   __syncwarp();
-  float c3[2][4];
-#pragma unroll
+  // sample 16 t + rr sits on lane 4 (rr % 8), columns 0..1, in c3[0..1] (rr < 8)
+  // or c3[2..3] of tile t; the tile loop is rolled to keep the code small
+  const int rr = lane & 15, src = 4 * (rr & 7);
+  const bool hi_r = rr >= 8;
+  float y0 = 0.f, y1 = 0.f;
+#pragma unroll 1
   for (int t = 0; t < 2; ++t) {
+    float c3[4];
     uint32_t xa[4];
     load_a(X, 8, t, 0, g, q, xa);
     uint32_t h1[4][4];  // layer-2 A fragments, k-steps 0..3
@@ -200,8 +205,8 @@ __device__ __forceinline__ void mlp_forward_staged(const uint32_t* __restrict__ 
       }
       relu_pack_a(c[0], c[1], h1[s]);
     }
-    c3[t][0] = c3[t][2] = b3.x;
-    c3[t][1] = c3[t][3] = b3.y;
+    c3[0] = c3[2] = b3.x;
+    c3[1] = c3[3] = b3.y;
 #pragma unroll
     for (int s3 = 0; s3 < 4; ++s3) {
       const float4 bb = __ldg(B2 + s3);
@@ -218,20 +223,16 @@ __device__ __forceinline__ void mlp_forward_staged(const uint32_t* __restrict__ 
       const uint32_t bw[2] = {(s3 & 1) ? f3.z : f3.x, (s3 & 1) ? f3.w : f3.y};
       uint32_t a3[4];
       relu_pack_a(c2[0], c2[1], a3);
-      mma_bf16(c3[t], a3, bw);
+      mma_bf16(c3, a3, bw);
+    }
+    const float v0 = __shfl_sync(kFull, c3[0], src), v1 = __shfl_sync(kFull, c3[1], src);
+    const float v2 = __shfl_sync(kFull, c3[2], src), v3 = __shfl_sync(kFull, c3[3], src);
+    if ((lane >> 4) == t) {
+      y0 = hi_r ? v2 : v0;
+      y1 = hi_r ? v3 : v1;
     }
   }
   __syncwarp();
-  // sample 16 t + rr sits on lane 4 (rr % 8), columns 0..1, in c3[t][0..1] (rr < 8) or c3[t][2..3]
-  const int rr = lane & 15, src = 4 * (rr & 7);
-  float v[2][4];
-#pragma unroll
-  for (int tt = 0; tt < 2; ++tt)
-#pragma unroll
-    for (int i = 0; i < 4; ++i) v[tt][i] = __shfl_sync(kFull, c3[tt][i], src);
-  const bool hi_t = lane >= 16, hi_r = rr >= 8;
-  const float y0 = hi_t ? (hi_r ? v[1][2] : v[1][0]) : (hi_r ? v[0][2] : v[0][0]);
-  const float y1 = hi_t ? (hi_r ? v[1][3] : v[1][1]) : (hi_r ? v[0][3] : v[0][1]);
   out[0] = y0 * p[kOffYsig] + p[kOffYmu];
   out[1] = y1 * p[kOffYsig + 1] + p[kOffYmu + 1];
 }
