@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0, help="tracers in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="gc_doubledipole_1M",
+                    choices=["gc_doubledipole_1M", "harris_adaptive_262k"],
+                    help="gc_doubledipole_1M: the headline metric; harris_adaptive_262k: the batching comparison")
     return ap.parse_args()
 
 
@@ -319,11 +322,84 @@ def run_ours(args, rank, ws, dist):
     print(json.dumps(line), flush=True)
 
 
+def advance_all(ens, kind, delta):
+    """Advance and resume tracers stopped by a full row buffer until all are
+    done (rows are reset on the device, not downloaded); returns summed stats."""
+    tot = {"accepted": 0, "rejected": 0, "kernel_ms": 0.0, "kernel_launches": 0, "switches": 0, "done": 0}
+    st = ens.advance(kind, delta)
+    while True:
+        for k in tot:
+            tot[k] += st[k]
+        if tot["done"] >= ens.n:
+            return tot
+        ens.ctx.check(ens.ctx.L.rapt_rows_download(ens.ctx.h, None, None, None, None, None, 1), "reset rows")
+        st = ens.advance_resume(kind)
+
+
+def run_config3(args, rank, ws, dist):
+    """Batching comparison on the Harris-sheet Adaptive ensemble (262,144
+    protons, durations log-uniform 1-300 s): the default persistent grid, the
+    autotuned launch shape with graph replay, and the unbatched pattern (one
+    launch sequence per tracer) on an evenly spaced sample."""
+    from rapt_gb300 import Ensemble, workloads as W, autotune as A, _native as N
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx = N.Context(dev)
+    w = W.config3(seed=rank)
+    n = len(w["mass"])
+    sim = float(np.sum(w["delta"]))
+    # autotune on a 16k sample advanced by a tenth of its durations
+    ws_ = A.sample(w, 16384)
+    es = Ensemble.from_workload(ws_, "adaptive", max_rows=1024, max_switch=64, ctx=ctx)
+    best, table = A.tune(es, "adaptive", ws_["delta"] / 10, use_cache=False)
+    del es
+    ens = Ensemble.from_workload(w, "adaptive", max_rows=1024, max_switch=64, ctx=ctx)
+    init = {k: v.copy() for k, v in ens.h.items()}
+    res = {}
+    for name, shape in (("default", {}), ("tuned", best)):
+        cfg = dict(w["params"])
+        cfg.update(shape)
+        ens.configure(**{k: 0 for k in ("threads_per_block", "blocks_per_sm", "use_graph")})
+        ens.configure(**cfg)
+        for k, v in init.items():
+            ens.h[k][...] = v
+        ens.upload()
+        ens.adaptive_init()
+        barrier(dist)
+        st = advance_all(ens, "adaptive", w["delta"])
+        dev_s = allmax(dist, st["kernel_ms"] * 1e-3)
+        res[name] = {"shape": shape or "128 threads, max blocks/SM, no graph", "device_s": dev_s,
+                     "accepted_per_s": allsum(dist, st["accepted"]) / dev_s,
+                     "tracer_seconds_per_s": allsum(dist, sim) / dev_s, "switches": int(st["switches"]),
+                     "kernel_launches": int(st["kernel_launches"])}
+    # unbatched: one launch sequence per tracer, on a 256-tracer sample
+    sm = A.sample(w, 256)
+    e1 = Ensemble.from_workload(sm, "adaptive", max_rows=1024, max_switch=64, ctx=ctx, per_tracer_launches=1)
+    st = advance_all(e1, "adaptive", sm["delta"])
+    sim1 = float(np.sum(sm["delta"]))
+    res["per_tracer_launches"] = {"sample_tracers": len(sm["mass"]), "device_s": st["kernel_ms"] * 1e-3,
+                                  "accepted_per_s": st["accepted"] / (st["kernel_ms"] * 1e-3),
+                                  "tracer_seconds_per_s": sim1 / (st["kernel_ms"] * 1e-3),
+                                  "kernel_launches": int(st["kernel_launches"])}
+    if rank != 0:
+        return
+    line = {"metric": "Adaptive tracer-seconds/s, batched graph vs per-tracer launches", "workload": "harris_adaptive_262k",
+            "value": res["tuned"]["tracer_seconds_per_s"], "unit": "tracer-seconds/s", "n_gpus": ws,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded, config-3 distributions)",
+            "config": {"workload": "harris_adaptive_262k", "tracers_per_gpu": n, "sim_tracer_seconds": sim,
+                       "gctimestep": 0.5, "rtol": 1e-8, "atol": 1e-8},
+            "results": res, "autotune": {"best": best, "table": table},
+            "speedup_batched_vs_per_tracer": res["tuned"]["tracer_seconds_per_s"] /
+            res["per_tracer_launches"]["tracer_seconds_per_s"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, ws, dist = dist_init(args)
     if args.impl == "reference":
         run_reference(args, rank, ws, dist)
+    elif args.workload == "harris_adaptive_262k":
+        run_config3(args, rank, ws, dist)
     else:
         run_ours(args, rank, ws, dist)
     if dist is not None:

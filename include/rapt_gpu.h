@@ -94,11 +94,15 @@ typedef struct {
   int32_t threads_per_block;     /* 0: default */
   int64_t max_steps_per_launch;  /* per-thread RK-step budget of one launch (0: default) */
   int32_t blocks_per_sm;         /* 0: default */
-  int32_t use_graph;             /* 1: replay the launch sequence as a captured CUDA graph */
+  int32_t use_graph;             /* 1: capture a chunk of launch rounds (queue resets, particle and
+                                    guiding-centre kernels, pending read-back) once per call as a CUDA
+                                    graph and replay it until no tracer is pending */
   int32_t collect;               /* 1: record step-size training samples (GC, DOPRI5; any form) */
   double learned_scale;          /* learned forms: multiplier on each MLP step proposal (0: 1) */
   int32_t learned_every;         /* learned forms: run the MLP on every k-th accepted step and reuse its
                                     correction in between (0 or 1: every step) */
+  int32_t per_tracer_launches;   /* 1: one launch sequence per tracer (the unbatched pattern, for
+                                    comparison); 0: one persistent grid for the whole ensemble */
 } rapt_config;
 
 /* Host-side SoA view of an ensemble. Any pointer may be NULL on download to

@@ -33,7 +33,7 @@ class RaptConfig(C.Structure):
                 ("form", C.c_int32), ("threads_per_block", C.c_int32),
                 ("max_steps_per_launch", C.c_int64), ("blocks_per_sm", C.c_int32),
                 ("use_graph", C.c_int32), ("collect", C.c_int32), ("learned_scale", C.c_double),
-                ("learned_every", C.c_int32)]
+                ("learned_every", C.c_int32), ("per_tracer_launches", C.c_int32)]
 
 
 class RaptHostState(C.Structure):

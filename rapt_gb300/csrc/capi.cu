@@ -454,6 +454,23 @@ __global__ void k_clear_rows_full(DevEnsemble E) {
 
 static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all, rapt_stats* stats, bool resume);
 
+// The ensemble restricted to tracer k (every per-tracer array offset by k, n = 1).
+static DevEnsemble ensemble_view(const DevEnsemble& E, int64_t k, int max_rows, int max_sw) {
+  DevEnsemble V = E;
+  V.n = 1;
+  V.mode += k; V.status += k; V.flags += k; V.t_int += k; V.t_row += k; V.tcur += k;
+  for (int i = 0; i < 6; ++i) V.s[i] += k;
+  V.mu += k; V.v += k; V.mass += k; V.charge += k;
+  V.naccept += k; V.nreject += k; V.nfcn += k; V.nswitch += k;
+  V.delta += k; V.seg_stop += k; V.seg_dt += k; V.seg_gm += k; V.seg_active += k; V.nseg += k;
+  V.rows += (size_t)k * max_rows * 7;
+  V.row_mode += (size_t)k * max_rows;
+  V.nrows += k;
+  V.sw_time += (size_t)k * max_sw;
+  V.sw_mode += (size_t)k * max_sw;
+  return V;
+}
+
 int rapt_advance(void* ctx, int kind, const double* delta, double delta_all, rapt_stats* stats) {
   Ctx* c = static_cast<Ctx*>(ctx);
   if (!c) return RAPT_ERR_INVALID;
@@ -516,23 +533,81 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
   int64_t launches = 0, kl = 1;
   const int max_rounds = 1000000;
   int round = 0;
-  for (; round < max_rounds; ++round) {
+  // one round: reset the queue heads and the pending count, run the particle
+  // kernel and the guiding-centre kernel over the ensemble view Ev
+  auto enqueue_round = [&](const DevEnsemble& Ev, int grid_p, int grid_g, int blk) -> int {
     CK(cudaMemsetAsync(c->scratch, 0, 3 * sizeof(unsigned long long), s));  // queue[2], pending
-    LaunchArgs a{E, P, c->scratch, 0, block, s};
+    LaunchArgs a{Ev, P, c->scratch, 0, blk, s};
     if (kind != RAPT_KIND_GC) {
-      a.grid = c->num_sms * bps_p;
+      a.grid = grid_p;
       CK(f32 ? T.particle32(a) : T.particle[tab](a));
       ++kl;
     }
     if (kind != RAPT_KIND_PARTICLE) {
-      a.grid = c->num_sms * bps_g;
+      a.grid = grid_g;
       CK(tab != 0 ? T.gc[tab](a) : (f32 ? T.gc32_lrn[lrn](a) : T.gc_lrn[lrn](a)));
       ++kl;
     }
-    ++launches;
+    return RAPT_OK;
+  };
+  auto read_pending = [&]() -> int {
     CK(cudaMemcpyAsync(c->h_pending, &c->scratch->pending, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (*c->h_pending == 0) break;
+    return RAPT_OK;
+  };
+  if (c->cfg.per_tracer_launches) {
+    // the unbatched pattern: every tracer gets its own launches (one warp),
+    // rounds repeated until it is done -- for comparison with the batched grid
+    for (int64_t k = 0; k < c->n; ++k) {
+      const DevEnsemble Ek = ensemble_view(E, k, c->max_rows, c->max_sw);
+      for (round = 0; round < max_rounds; ++round) {
+        int rc = enqueue_round(Ek, 1, 1, 32);
+        if (rc) return rc;
+        ++launches;
+        rc = read_pending();
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(s));
+        if (*c->h_pending == 0) break;
+      }
+      if (round >= max_rounds) break;
+    }
+  } else if (c->cfg.use_graph) {
+    // capture kGraphRounds rounds and the pending read-back once, replay until done
+    constexpr int kGraphRounds = 4;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = RAPT_OK;
+    const int64_t kl0 = kl;
+    for (int r = 0; r < kGraphRounds && rc == RAPT_OK; ++r)
+      rc = enqueue_round(E, c->num_sms * bps_p, c->num_sms * bps_g, block);
+    if (rc == RAPT_OK) rc = read_pending();
+    cudaError_t ec = cudaStreamEndCapture(s, &graph);
+    if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+    if (ec != cudaSuccess) return fail(c, RAPT_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ec));
+    ec = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ec != cudaSuccess) return fail(c, RAPT_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ec));
+    const int64_t per_replay = kl - kl0;
+    kl = kl0;
+    for (round = 0; round < max_rounds; round += kGraphRounds) {
+      ec = cudaGraphLaunch(exec, s);
+      if (ec == cudaSuccess) ec = cudaStreamSynchronize(s);
+      if (ec != cudaSuccess) { cudaGraphExecDestroy(exec); return fail(c, RAPT_ERR_CUDA, "graph launch: %s", cudaGetErrorString(ec)); }
+      launches += kGraphRounds;
+      kl += per_replay;
+      if (*c->h_pending == 0) break;
+    }
+    cudaGraphExecDestroy(exec);
+  } else {
+    for (; round < max_rounds; ++round) {
+      int rc = enqueue_round(E, c->num_sms * bps_p, c->num_sms * bps_g, block);
+      if (rc) return rc;
+      ++launches;
+      rc = read_pending();
+      if (rc) return rc;
+      CK(cudaStreamSynchronize(s));
+      if (*c->h_pending == 0) break;
+    }
   }
   CK(cudaEventRecord(c->ev1, s));
   Scratch hs;
