@@ -149,3 +149,29 @@ def test_learned_ab_against_plain(ctx, trained, oracle):
     # run) within 3x of the plain controller's, per tracer at the median
     for r in (le, lf):
         assert r["glob_med"] < 3 * pl["glob_med"] and r["glob_max"] < 10 * pl["glob_max"], report
+
+
+def test_forms_error_at_bench_workload(ctx, trained, oracle):
+    """2,048 tracers of the 1M benchmark ensemble, one benchmark step (1 s):
+    relative final-position error of every form against the FP64 oracle."""
+    from tests._util import oracle_tracers
+    w0, p, info = trained
+    w = W.subsample(W.gc_bench(1 << 20), np.arange(0, 1 << 20, 512))
+    f, cfg, tr = oracle_tracers(oracle, w, "gc")
+    oracle.batch_advance(f, cfg, 1, tr, 1.0)
+    ctx.mlp_set_params(p)
+    errs = {}
+    for form in (PLAIN, FP32, LEARNED, LEARNED_FP32):
+        e = gpu_ensemble(w, "gc", max_rows=4, form=form, learned_scale=info["scale"])
+        e.advance("gc", 1.0)
+        h = e.download()
+        assert np.all(h["status"] == 0)
+        pos, _ = rel_state_error(h["s"], tr["s"], 4)
+        errs[form] = (float(np.median(pos)), float(np.percentile(pos, 99)), float(pos.max()))
+    print("bench-workload errors (median, p99, max)", errs)
+    # plain: rounding-level differences (a few orbits amplify them to ~1e-9)
+    assert errs[PLAIN][0] < 1e-12 and errs[PLAIN][2] < 1e-8
+    assert errs[FP32][0] < 1e-8 and errs[FP32][2] < 1e-6
+    # the learned forms take other (larger) steps: their difference is the
+    # integration error at rtol 1e-8; the target is 1e-6 for every tracer
+    assert errs[LEARNED_FP32][2] < 1e-6 and errs[LEARNED][2] < 1e-6
