@@ -234,12 +234,13 @@ __global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P,
 
 template <int M, int LRN = 0>
 // LRN: 0 plain controller, 1 training-sample collection, 2 MLP step proposals.
-// 16 blocks of 128 threads per SM (32 registers, the rest spilled to L1/L2):
-// the float-float stages are long dependent FP32 chains, and on GB300 more
-// resident warps hide their latency better than registers avoid the spills
-// (measured at 262k tracers: 1.11e8 accepted steps/s at 1 block/SM, 1.93e8 at
-// 8, 2.37e8 at 16).
-__global__ void __launch_bounds__(128, 16) k_gc32(DevEnsemble E, KParams P, Scratch* S) {
+// 12 (plain controller) or 16 (MLP proposals) blocks of 128 threads per SM,
+// 40 or 32 registers with the rest spilled: the float-float stages are long
+// dependent FP32 chains, and on GB300 more resident warps hide their latency
+// better than registers avoid the spills. Measured on the 1M guiding-centre
+// step: 1 block/SM 1.11e8 accepted steps/s, 8: 4.41e8, 12: 4.53e8, 16: 4.27e8
+// (the MLP variant: 12: 3.45e8, 16: 3.50e8).
+__global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E, KParams P, Scratch* S) {
   int64_t idx = -1;
   bool exhausted = false;
   long long budget = P.budget;
