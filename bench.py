@@ -53,8 +53,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="gc_doubledipole_1M",
-                    choices=["gc_doubledipole_1M", "harris_adaptive_262k"],
-                    help="gc_doubledipole_1M: the headline metric; harris_adaptive_262k: the batching comparison")
+                    choices=["gc_doubledipole_1M", "harris_adaptive_262k", "earthdipole_particles", "compressed_adaptive"],
+                    help="gc_doubledipole_1M: the headline metric; harris_adaptive_262k: the batching comparison; "
+                         "earthdipole_particles (config 4) and compressed_adaptive (config 5): form comparisons "
+                         "on --n tracers")
+    ap.add_argument("--forms", default="plain,fp32,learned,learned_fp32",
+                    help="comma-separated forms to time (plain, fp32, learned, learned_fp32)")
     return ap.parse_args()
 
 
@@ -228,10 +232,13 @@ def run_ours(args, rank, ws, dist):
         ens.upload()
 
     results = {}
+    forms = [(nm, f) for nm, f in FORMS if nm in args.forms.split(",")]
+    if "plain" not in dict(forms) or HEADLINE not in dict(forms):
+        raise SystemExit("--forms must include plain and %s" % HEADLINE)
     barrier(dist)
     clk = Clocks(dev) if rank == 0 else None
     t_all = time.perf_counter()
-    for name, form in FORMS:
+    for name, form in forms:
         reset()
         ens.configure(form=form, learned_scale=fit["scale"], collect=0)
         for _ in range(args.warmup):
@@ -393,6 +400,65 @@ def run_config3(args, rank, ws, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_forms_workload(args, rank, ws, dist):
+    """Form comparison on config 4 (particles in the Earth dipole, 50
+    gyro-periods, DOP853) or config 5 (Adaptive in the compressed dipole with its
+    induced E, 200 s), on --n tracers: device time, accepted and rejected steps,
+    simulated tracer-seconds/s of each form. For config 5 the step MLP is
+    trained first (guiding-centre segments use it; particle segments run the
+    plain controller)."""
+    from rapt_gb300 import Ensemble, workloads as W, _native as N
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx = N.Context(dev)
+    if args.n != (1 << 20):
+        n = args.n
+    else:
+        n = (1 << 18) if args.workload == "earthdipole_particles" else (1 << 16)
+    if args.workload == "earthdipole_particles":
+        w = W.subsample(W.config4(seed=rank), np.arange(0, 1 << 20, max(1, (1 << 20) // n))[:n])
+        kind, delta, rows = "particle", w["delta"], 520
+        forms = [("plain", 0), ("fp32", 1)]
+        scale = 1.0
+    else:
+        w = W.subsample(W.config5(seed=rank), np.arange(0, 1 << 20, max(1, (1 << 20) // n))[:n])
+        kind, delta, rows = "adaptive", 200.0, 1024
+        forms = list(FORMS)
+        params, fit = train_step_model(ctx)
+        ctx.mlp_set_params(params)
+        scale = fit["scale"]
+    ens = Ensemble.from_workload(w, kind, max_rows=rows, max_switch=64, ctx=ctx)
+    init = {k: v.copy() for k, v in ens.h.items()}
+    sim = float(np.sum(np.broadcast_to(delta, (len(w["mass"]),))))
+    res = {}
+    for name, form in forms:
+        for k, v in init.items():
+            ens.h[k][...] = v
+        ens.upload()
+        if kind == "adaptive":
+            ens.adaptive_init()
+        ens.configure(form=form, learned_scale=scale)
+        barrier(dist)
+        st = advance_all(ens, kind, delta)
+        h = ens.download()
+        dev_s = allmax(dist, st["kernel_ms"] * 1e-3)
+        res[name] = {"device_s": dev_s, "accepted": int(st["accepted"]), "rejected": int(st["rejected"]),
+                     "reject_rate": st["rejected"] / max(st["accepted"], 1),
+                     "accepted_per_s": allsum(dist, st["accepted"]) / dev_s,
+                     "tracer_seconds_per_s": allsum(dist, sim) / dev_s, "switches": int(st["switches"]),
+                     "failed": int(np.count_nonzero(h["status"])),
+                     "status_counts": {int(k): int(v) for k, v in zip(*np.unique(h["status"], return_counts=True))},
+                     "naccept_per_tracer": {"median": float(np.median(h["naccept"])),
+                                            "p99": float(np.percentile(h["naccept"], 99)),
+                                            "max": int(h["naccept"].max())}}
+    if rank != 0:
+        return
+    plain = res["plain"]
+    for r in res.values():
+        r["tracer_seconds_per_s_vs_plain"] = r["tracer_seconds_per_s"] / plain["tracer_seconds_per_s"]
+    print(json.dumps({"workload": args.workload, "tracers_per_gpu": len(w["mass"]), "n_gpus": ws,
+                      "kind": kind, "sim_tracer_seconds": sim, "results": res}), flush=True)
+
+
 def main():
     args = parse()
     rank, ws, dist = dist_init(args)
@@ -400,6 +466,8 @@ def main():
         run_reference(args, rank, ws, dist)
     elif args.workload == "harris_adaptive_262k":
         run_config3(args, rank, ws, dist)
+    elif args.workload in ("earthdipole_particles", "compressed_adaptive"):
+        run_forms_workload(args, rank, ws, dist)
     else:
         run_ours(args, rank, ws, dist)
     if dist is not None:
