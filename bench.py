@@ -40,6 +40,11 @@ UNIT = "accepted steps/s"
 # 446 flops (7-point stencil of 7 B evaluations) + 275 flops of stage
 # combination, error norm and control; rsqrt/sqrt/div/pow count as one flop each.
 FLOPS_PER_ACCEPTED_STEP = 6 * 446 + 275 + 6 * 23 + 4
+# DRAM traffic of one launch of the learned FP32 kernel per tracer and simulated
+# second (dram__bytes_read.sum + dram__bytes_write.sum of one ncu --set full
+# capture of the 262,144-tracer case: 198.8 + 221.5 GB), scaled by tracer count:
+# local-memory spill traffic of the 32-register, 16-blocks/SM configuration.
+TRAFFIC_PER_TRACER_SECOND = (198.8e9 + 221.5e9) / 262144
 
 
 def parse():
@@ -311,7 +316,10 @@ def run_ours(args, rank, ws, dist):
                            "samples": int(sum(c["samples"] for c in fit["collect"])),
                            "calibration": fit["calibration"][-1], "losses": fit["losses"][-1]},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": achieved / fp64_peak, "traffic": None, "kernel": "k_gc32 (learned)",
+                         "frac": achieved / fp64_peak, "traffic": TRAFFIC_PER_TRACER_SECOND * n,
+                         "traffic_note": "bytes per launch, scaled from a 262,144-tracer ncu capture; "
+                                         "spill traffic (algorithmic state traffic ~464 B per tracer)",
+                         "kernel": "k_gc32 (learned)",
                          "peak_source": "measured in-run: FP64 FMA chains (rapt_measure_peaks)",
                          "flops_per_accepted_step": FLOPS_PER_ACCEPTED_STEP,
                          "flops_note": "algorithmic FP64-equivalent flops of one DOPRI5 step",
