@@ -13,7 +13,7 @@ this file's gradients and by the kernels' agreement with this file.
 
 Parameter vector (floats): W1T[64][16] b1[64] W2T[64][64] b2[64] W3T[8][64]
 b3[8] | xmu[16] xsig[16] ymu[8] ysig[8]. Sample: 16 raw features, the step
-target, the switch label (-1: none).
+target (NaN: none), the switch label (-1: none).
 """
 import numpy as np
 
@@ -81,10 +81,11 @@ def loss_and_grad(params, samples, switch_weight=1.0, exact=False):
     B = s.shape[0]
     _, v = forward(params, s[:, :16], exact)
     X, H1, H2, O, W2, W3 = v["X"], v["H1"], v["H2"], v["O"], v["W2"], v["W3"]
-    tn = (s[:, 16].astype(np.float64) - d["ymu"][0]) / d["ysig"][0]
+    tg = s[:, 16].astype(np.float64)
+    tn = (np.nan_to_num(tg) - d["ymu"][0]) / d["ysig"][0]
     lab = s[:, 17].astype(np.float64)
     has = lab >= 0
-    d0 = O[:, 0] - tn
+    d0 = np.where(np.isnan(tg), 0.0, O[:, 0] - tn)  # NaN target: switch-labelled sample
     sg = 1.0 / (1.0 + np.exp(-O[:, 1]))
     d1 = np.where(has, switch_weight * (sg - lab), 0.0)
     o1 = O[:, 1]
@@ -134,4 +135,5 @@ def _loss64(p, samples, switch_weight):
     has = lab >= 0
     o1 = O[:, 1]
     l1 = np.where(has, switch_weight * (np.maximum(o1, 0) - o1 * lab + np.log1p(np.exp(-np.abs(o1)))), 0.0)
-    return 0.5 * np.mean((O[:, 0] - tn) ** 2), np.mean(l1)
+    l0 = np.where(np.isnan(tn), 0.0, (O[:, 0] - np.nan_to_num(tn)) ** 2)
+    return 0.5 * np.mean(l0), np.mean(l1)

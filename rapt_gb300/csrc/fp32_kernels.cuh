@@ -413,6 +413,7 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
           h = hnew;
         }
         lr.on_accept(P, idx, nacc, hstep, err, errprev, h, hmax, was_last, rej_before, nst - nacc_int <= 8,
+                     (flags & RAPT_FLAG_CHECK_ADIABATICITY) != 0,
                      y[0].hi, y[1].hi, y[2].hi,
                      y[3].hi, vs, 1.0 - (xend - rt) / hmax);
       } else {
@@ -433,8 +434,10 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
       t_row = rt;
       tcur = rt;
       put_row(E, P, idx, nrows, rt, s, 4, RAPT_MODE_GC);
-      if ((flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE &&
-          !gc_isadiabatic<M>(P, t_row, s, mu, mass, charge)) {
+      const bool row_chk = (flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE;
+      const bool nonadi = row_chk && !gc_isadiabatic<M>(P, t_row, s, mu, mass, charge);
+      if (row_chk) lr.on_row(P, nonadi);
+      if (nonadi) {
         if (P.kind == RAPT_KIND_ADAPTIVE) {
           double s6[6];
           gc_to_particle<M>(P.f, t_row, s, mu, mass, charge, s6);

@@ -1,9 +1,9 @@
 // mlp.cu -- training and batch inference of the step-size / switch MLP on the
 // tensor cores (mma.sync BF16, FP32 accumulation), plus Adam and weight packing.
 //
-// Loss per sample: 0.5 (o0 - t0)^2 on the normalised step target plus
-// switch_weight * BCE(sigmoid(o1), label) where a label exists (label >= 0);
-// the batch loss is the mean. Backward pass per 32-sample chunk (one warp):
+// Loss per sample: 0.5 (o0 - t0)^2 on the normalised step target (where it is
+// not NaN) plus switch_weight * BCE(sigmoid(o1), label) where a label exists
+// (label >= 0); the batch loss is the mean. Backward pass per 32-sample chunk (one warp):
 //   dO -> dW3, db3 (CUDA cores), dZ2 = (dO W3^T) * [H2 > 0] (BF16),
 //   dW2 = H1^T dZ2, dH1 = dZ2 W2^T, dZ1 = dH1 * [H1 > 0], dW1 = X^T dZ1
 // (mma.sync), with the chunk's weight gradients summed in shared memory and
@@ -87,9 +87,12 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_mlp_train(TrainArgs a) {
     // ---- loss and output gradient
     float d0 = 0.f, d1 = 0.f;
     if (valid) {
-      const float tn = (smp[16] - p[kOffYmu]) / p[kOffYsig];
-      d0 = o[0] - tn;
-      l0sum += 0.5 * (double)d0 * d0;
+      const float tg = smp[16];  // NaN: no step target (switch-labelled sample)
+      if (tg == tg) {
+        const float tn = (tg - p[kOffYmu]) / p[kOffYsig];
+        d0 = o[0] - tn;
+        l0sum += 0.5 * (double)d0 * d0;
+      }
       const float lab = smp[17];
       if (lab >= 0.f) {
         const float sg = 1.f / (1.f + __expf(-o[1]));

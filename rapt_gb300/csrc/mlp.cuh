@@ -268,18 +268,18 @@ struct StepLearner {
   int since;                                // accepted steps since the last network call
   double hbase;                             // collect: the controller's step after the sampled step
   double hcont;                             // learned: the step wanted before the interval-end clip
-  bool want, pend, have_prop;
+  bool want, pend, pend_sw, have_prop;
   uint32_t* sm;
 
   __device__ __forceinline__ void init(const KParams& P) {
-    want = pend = have_prop = false;
+    want = pend = pend_sw = have_prop = false;
     rlast = 1.f;
     since = 0;
     sm = LRN ? rapt_dyn_smem + (threadIdx.x >> 5) * warp_words(P.collect != 0) : nullptr;
   }
   // Per-tracer constants; vs is the speed, pitch scale converts ppar to cos(pitch).
   __device__ __forceinline__ void load(double mass, double charge, double vs, double ppar_unit) {
-    want = pend = have_prop = false;
+    want = pend = pend_sw = have_prop = false;
     rlast = 1.f;
     since = 0;
     if constexpr (LRN != 0) {
@@ -299,22 +299,27 @@ struct StepLearner {
   // ended an output interval gives no sample; the learned form continues the
   // next interval with the step wanted before the clip (in place of HINIT).
   // `allow` switches the proposals off (the plain controller takes over) for
-  // the rest of an output interval that has seen many rejections.
+  // the rest of an output interval that has seen many rejections. A step that
+  // ends an interval whose row gets an adiabaticity check (`row_check`) stages
+  // its features for a switch-labelled sample (on_row).
   __device__ __forceinline__ void on_accept(const KParams& P, int64_t idx, long long nacc, double h, double err,
                                             double errprev, double& hnew, double hmax, bool last, bool rej_before,
-                                            bool allow, float x, float y, float z, float ppar, double vs,
-                                            double progress) {
+                                            bool allow, bool row_check, float x, float y, float z, float ppar,
+                                            double vs, double progress) {
     if constexpr (LRN == 0) return;
+    bool coll = false, coll_sw = false;
     if (last) {
       if constexpr (LRN == 2) {
         hnew = hcont;
         have_prop = true;
       }
-      return;
+      coll_sw = (LRN == 1 || P.collect) && row_check;
+      if (!coll_sw) return;
+    } else {
+      coll = (LRN == 1 || P.collect) &&
+             (mix64((uint64_t)idx * 0x100000001b3ull + (uint64_t)nacc) & P.samp_mask) == 0;
     }
-    const bool coll = (LRN == 1 || P.collect) &&
-                      (mix64((uint64_t)idx * 0x100000001b3ull + (uint64_t)nacc) & P.samp_mask) == 0;
-    bool inf = LRN == 2 && allow;
+    bool inf = LRN == 2 && allow && !last;
     if constexpr (LRN == 2) {
       if (inf && P.learn_every > 1 && ++since < P.learn_every) {
         // between network calls: the last correction on the controller's step
@@ -324,7 +329,7 @@ struct StepLearner {
         inf = false;
       }
     }
-    if (!coll && !inf) return;
+    if (!coll && !coll_sw && !inf) return;
     float f[16];
     const float r = sqrtf(x * x + y * y + z * z);
     f[0] = __logf((float)(fabs(h) * vs) / r);
@@ -344,11 +349,12 @@ struct StepLearner {
     f[14] = 0.f;
     f[15] = 0.f;
     const int lane = threadIdx.x & 31;
-    if (coll) {
+    if (coll || coll_sw) {
       float* row = reinterpret_cast<float*>(sm + kRawOff) + lane * 16;
 #pragma unroll
       for (int i = 0; i < 16; ++i) row[i] = f[i];
-      pend = true;
+      pend = coll;
+      pend_sw = coll_sw;
       hbase = hnew;
     }
     if constexpr (LRN == 2) {
@@ -376,6 +382,24 @@ struct StepLearner {
         for (int i = 0; i < 16; ++i) dst[i] = row[i];
         dst[16] = y0;
         dst[17] = -1.f;
+      }
+    }
+  }
+  // Collect: the adiabaticity check of the row that ended the interval labels
+  // the staged sample (label 1: the tracer switches to particle mode); its step
+  // target is NaN (no step follows the row in this interval).
+  __device__ __forceinline__ void on_row(const KParams& P, bool switches) {
+    if constexpr (LRN != 0) {
+      if (!pend_sw) return;
+      pend_sw = false;
+      const unsigned long long pos = atomicAdd(P.samp_count, 1ull);
+      if (pos < (unsigned long long)P.samp_cap) {
+        const float* row = reinterpret_cast<const float*>(sm + kRawOff) + (threadIdx.x & 31) * 16;
+        float* dst = P.samp + pos * kSampleStride;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) dst[i] = row[i];
+        dst[16] = __int_as_float(0x7fc00000);
+        dst[17] = switches ? 1.f : 0.f;
       }
     }
   }

@@ -698,6 +698,7 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
             h = hnew;
           }
           lr.on_accept(P, idx, nacc, hstep, err, errprev, h, hmax, was_last, rej_before, nst - nacc_int <= 8,
+                     (flags & RAPT_FLAG_CHECK_ADIABATICITY) != 0,
                      (float)y[0], (float)y[1],
                        (float)y[2], (float)y[3], vs, 1.0 - (xend - rt) / hmax);
         } else {
@@ -741,8 +742,10 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
       t_row = rt;
       tcur = rt;
       put_row(E, P, idx, nrows, rt, y, 4, RAPT_MODE_GC);
-      if ((flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE &&
-          !gc_isadiabatic<M>(P, t_row, y, mu, mass, charge)) {
+      const bool row_chk = (flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE;
+      const bool nonadi = row_chk && !gc_isadiabatic<M>(P, t_row, y, mu, mass, charge);
+      if (row_chk) lr.on_row(P, nonadi);
+      if (nonadi) {
         if (P.kind == RAPT_KIND_ADAPTIVE) {
           double s6[6];
           gc_to_particle<M>(P.f, t_row, y, mu, mass, charge, s6);

@@ -23,6 +23,13 @@ Features (computed on the device after each accepted step):
   6 log10(m / m_e)        7 log10(gamma - 1)      8 cos(pitch) = ppar / (gamma m v)
   9 log(r / Re)          10 z / r                11 position in the output interval
  12 output interval / |h|                        13 step followed a rejection
+
+Switch head: in Adaptive runs the guiding-centre kernels also record, at every
+output row that gets an adiabaticity check, the features of the step that
+ended the interval with label 1 if the check fails (the tracer switches to
+particle mode) and no step target; the head is trained with a masked binary
+cross-entropy and reported (``switch_metrics``). The kernels keep the exact
+check at every row, so switching follows the reference either way.
 """
 import numpy as np
 
@@ -76,8 +83,10 @@ def set_normalisation(params, samples):
     p[n0 + 16:n0 + 32] = sig
     ymu = np.zeros(8)
     ysig = np.ones(8)
-    ymu[0] = s[:, 16].mean()
-    ysig[0] = max(s[:, 16].std(), 1e-6)
+    t = s[:, 16][np.isfinite(s[:, 16])]  # switch-labelled samples have no step target
+    if t.size:
+        ymu[0] = t.mean()
+        ysig[0] = max(t.std(), 1e-6)
     p[n0 + 32:n0 + 40] = ymu
     p[n0 + 40:n0 + 48] = ysig
     return p
@@ -167,6 +176,7 @@ def calibrate(ctx, samples, margins=np.linspace(0.0, 1.0, 201)):
     for the plain controller's hnew. Returns a dict with the margin, the
     proposal scale exp(-c) for rapt_config.learned_scale and both efficiencies."""
     s = np.asarray(samples, np.float32)
+    s = s[np.isfinite(s[:, 16])]
     pred = ctx.mlp_forward(s[:, :16])[:, 0].astype(np.float64)
     y = s[:, 16].astype(np.float64)
     eff = np.array([np.mean(np.exp(pred - c - y) * (pred - c <= y)) for c in margins])
@@ -176,6 +186,22 @@ def calibrate(ctx, samples, margins=np.linspace(0.0, 1.0, 201)):
     return {"margin": c, "scale": float(np.exp(-c)), "eff_learned": float(eff[k]), "eff_plain": plain,
             "accept_learned": float(np.mean(pred - c <= y)), "accept_plain": float(np.mean(y >= 0)),
             "resid_std": float(np.std(pred - y)), "target_std": float(np.std(y))}
+
+
+def switch_metrics(ctx, samples, threshold=0.5):
+    """Switch head on switch-labelled samples [n][18] (label >= 0) with the
+    network loaded in ctx: accuracy, recall and precision of the prediction
+    sigmoid(logit) > threshold, against the base rate of switches."""
+    s = np.asarray(samples, np.float32)
+    s = s[s[:, 17] >= 0]
+    if len(s) == 0:
+        return {"n": 0}
+    p = 1.0 / (1.0 + np.exp(-ctx.mlp_forward(s[:, :16])[:, 1].astype(np.float64)))
+    y = s[:, 17] > 0.5
+    pr = p > threshold
+    tp = int(np.sum(pr & y))
+    return {"n": int(len(s)), "base_rate": float(y.mean()), "accuracy": float(np.mean(pr == y)),
+            "recall": tp / max(int(y.sum()), 1), "precision": tp / max(int(pr.sum()), 1)}
 
 
 def save(path, params):

@@ -175,3 +175,28 @@ def test_forms_error_at_bench_workload(ctx, trained, oracle):
     # the learned forms take other (larger) steps: their difference is the
     # integration error at rtol 1e-8; the target is 1e-6 for every tracer
     assert errs[LEARNED_FP32][2] < 1e-6 and errs[LEARNED][2] < 1e-6
+
+
+def test_switch_head_on_harris_adaptive(ctx):
+    """Switch-labelled samples from Adaptive runs in the Harris sheet (even
+    tracers train, odd tracers test): the trained switch head against the
+    majority-class predictor. The kernels keep the exact check either way."""
+    w = W.subsample(W.config3(), np.arange(0, 262144, 32))
+    tr = W.subsample(w, np.arange(0, len(w["mass"]), 2))
+    te = W.subsample(w, np.arange(1, len(w["mass"]), 2))
+    ctx.mlp_samples_reserve(1 << 21, 0)
+    e = gpu_ensemble(tr, "adaptive", max_rows=4096, max_switch=64, collect=1)
+    e.advance("adaptive", tr["delta"] / 3)
+    s = ctx.mlp_samples_download()
+    lab = s[:, 17]
+    assert np.all(np.isnan(s[lab >= 0, 16])) and np.all(np.isfinite(s[lab < 0, 16]))
+    n_sw = int(np.sum(lab >= 0))
+    assert n_sw > 1000 and 0 < np.mean(lab[lab >= 0]) < 1, (n_sw, np.mean(lab[lab >= 0]))
+    p, losses = learned.train(ctx, steps=2000, batch=4096, lr=2e-3, seed=3)
+    ctx.mlp_samples_reserve(1 << 21, 0)
+    e = gpu_ensemble(te, "adaptive", max_rows=4096, max_switch=64, collect=1)
+    e.advance("adaptive", te["delta"] / 3)
+    m = learned.switch_metrics(ctx, ctx.mlp_samples_download())
+    print("switch head", m, "losses", losses)
+    majority = max(m["base_rate"], 1 - m["base_rate"])
+    assert m["accuracy"] > majority, m

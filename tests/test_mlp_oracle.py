@@ -14,6 +14,10 @@ def _problem(seed=0, n=96):
     feats[:, 14:] = 0
     target = (np.sin(feats[:, 0]) + 0.3 * feats[:, 3]).astype(np.float32)
     lab = np.where(rng.random(n) < 0.5, (feats[:, 1] > 1).astype(np.float32), -1.0).astype(np.float32)
+    # a fifth of the samples carry only a switch label (no step target)
+    sw_only = rng.random(n) < 0.2
+    target[sw_only] = np.nan
+    lab[sw_only] = (feats[sw_only, 2] > 0).astype(np.float32)
     samples = np.column_stack([feats, target, lab]).astype(np.float32)
     p = learned.set_normalisation(p, samples)
     # nonzero biases so every parameter block matters
