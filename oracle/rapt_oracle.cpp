@@ -57,6 +57,8 @@ void orc_config_default(orc_config* c) {
   c->tableau = 0;
   c->gc_eom = 0;
   c->nsteps = 500;
+  c->bounceres = 10;
+  c->flres = 50;
   c->rkf_tol = 1e-3;
   c->rkf_hmin = 1e-12;
 }
@@ -954,8 +956,9 @@ int orc_particle_advance(const orc_field* f, const orc_config* c, orc_tracer* p,
 int orc_gc_advance(const orc_field* f, const orc_config* c, orc_tracer* g, double delta,
                    int check_adiabaticity, double* rows, int max_rows, int* nrows) {
   // GuidingCenter.advance, rapt/GuidingCenter.py:397-458 (dopri5 at :450)
-  if (!(c->gctimestep > 0)) { g->status = ORC_ST_BAD_INPUT; return 0; }
-  const double dt = c->gctimestep;
+  // cadence: GCtimestep, or the bounce period at the current state / bounceresolution (:443-446)
+  const double dt = c->gctimestep != 0 ? c->gctimestep : orc_gc_bounceperiod(f, g, c->flres) / c->bounceres;
+  if (!(dt > 0) || !std::isfinite(dt)) { g->status = ORC_ST_BAD_INPUT; return 0; }
   const double t0 = g->t;
   double rt = g->t;
   double y[4];

@@ -41,13 +41,15 @@ typedef struct {
 typedef struct {
   double rtol, atol;       /* params["solvertolerances"] */
   double cycres;           /* params["cyclotronresolution"] */
-  double gctimestep;       /* params["GCtimestep"] (> 0 required) */
+  double gctimestep;       /* params["GCtimestep"] (0: bounce-period cadence) */
   double epss, epst;       /* params["epss"], params["epst"] */
   int enforce_equatorial;  /* params["enforce equatorial"] */
   int tableau;             /* 0: DOP853 (particle) / DOPRI5 (GC); 1: RKF45 (rkf.py) */
   int gc_eom;              /* 0 TaoChanBrizard, 1 BrizardChan, 2 NorthropTeller */
   int nsteps;              /* SciPy ode nsteps (500) */
   double rkf_tol, rkf_hmin;/* RKF45 tableau: rkf.py tol and hmin */
+  double bounceres;        /* params["bounceresolution"]: GC cadence T_b / bounceres when gctimestep == 0 */
+  double flres;            /* params["fieldlineresolution"] */
 } orc_config;
 
 /* One tracer (a Particle or a GuidingCenter segment). */
@@ -121,6 +123,16 @@ int orc_particle_advance(const orc_field* f, const orc_config* c, orc_tracer* p,
                          int check_adiabaticity, double* rows, int max_rows, int* nrows);
 int orc_gc_advance(const orc_field* f, const orc_config* c, orc_tracer* g, double delta,
                    int check_adiabaticity, double* rows, int max_rows, int* nrows);
+
+/* Field lines and the bounce period (fieldline_oracle.cpp): GuidingCenter.bounceperiod
+ * (GuidingCenter.py:593-606), flutils.halfbouncepath (flutils.py:254-316), the
+ * (s, |B|) samples of Fieldline.trace (fieldline.py:37-107), and QAGS on test
+ * integrands (for pinning against scipy.integrate.quad). */
+double orc_gc_bounceperiod(const orc_field* f, const orc_tracer* g, double flres);
+double orc_halfbouncepath(const orc_field* f, const double* tpos, double Bm, double flres, int* npts);
+int orc_fieldline_sB(const orc_field* f, const double* tpos, double Bm, double flres, double* s, double* B,
+                     int cap);
+double orc_qags_test(int which, double a, double b, double epsabs, double epsrel, int limit, int* ier);
 
 /* Adaptive (rapt/Adaptive.py). init returns the starting tracer. advance writes
  * rows (with a per-row mode byte) and a switch log (time, new mode). */

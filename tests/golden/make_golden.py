@@ -291,6 +291,28 @@ def main():
     out["adaptive_harris_final"] = np.r_[a.trajlist[-1].trajectory[-1], np.zeros(7 - a.trajlist[-1].trajectory.shape[1])]
     out["adaptive_harris_nrows"] = np.array([len(s.trajectory) for s in a.trajlist])
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")
+    # bounce period (flutils.halfbouncepath, GuidingCenter.bounceperiod) and the
+    # bounce-period cadence of GuidingCenter.advance (GCtimestep = 0)
+    bp = []
+    for mid, fobj in ((0, ed), (1, ddf)):
+        for L, pa_deg, phi in ((5.0, 45, 180), (6.0, 15, 180), (4.5, 80, 90), (7.0, 30, 0), (5.5, 89.5, 45)):
+            tpos = np.array([0, L * Re * np.cos(np.radians(phi)), L * Re * np.sin(np.radians(phi)), 0.0])
+            Bm = fobj.magB(tpos) / np.sin(np.radians(pa_deg)) ** 2
+            bp.append((mid, L, pa_deg, phi, Bm, rapt.flutils.halfbouncepath(tpos, fobj, Bm)))
+    out["bounce_halfpath"] = np.array(bp)  # model id, L, pa, phi, Bm, S_b
+    gbp = []
+    for ke, pa_deg, L, mass, q in ((1e6, 45, 5.0, m_el, -e), (1e5, 30, 6.0, m_pr, e), (5e6, 70, 4.0, m_el, -e)):
+        pos = np.array([L * Re, 0, 0])
+        v = rapt.utils.speedfromKE(ke, mass)
+        g = rapt.GuidingCenter(pos, v, pa=pa_deg, t0=0, mass=mass, charge=q, field=ddf)
+        gbp.append(np.r_[pos, v, pa_deg, mass, q, g.bounceperiod()])
+    out["bounce_gc_period"] = np.array(gbp)  # pos(3), v, pa, mass, charge, T_b
+    pos = np.array([5 * Re, 0, 0])
+    v = rapt.utils.speedfromKE(1e6, m_el)
+    out["traj_gbounce_init"] = np.r_[pos, v, 45, m_el, -e]
+    run("gbounce", rapt.GuidingCenter(pos, v, pa=45, t0=0, mass=m_el, charge=-e, field=ddf), 0.5,
+        solvertolerances=(1e-8, 1e-8), GCtimestep=0)
+
     np.savez_compressed(dst, **out)
     print("wrote", dst, os.path.getsize(dst), "bytes,", len(out), "arrays")
 

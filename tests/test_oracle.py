@@ -180,3 +180,51 @@ def test_adaptive_harris(oracle):
     fin = GOLD["adaptive_harris_final"]
     n = 7 if tr.mode == 0 else 5
     assert np.allclose([tr.t, *tr.s[:n - 1]], fin[:n], rtol=1e-9)
+
+
+# ---------------------------------------------------------------- bounce period
+def test_qags_matches_scipy_quad(oracle):
+    """The QUADPACK QAGS restatement against scipy.integrate.quad (the routine
+    flutils.halfbouncepath calls), on singular, oscillatory and smooth integrands."""
+    quad = pytest.importorskip("scipy.integrate").quad
+    fs = {0: lambda x: 1 / np.sqrt(x), 1: lambda x: np.log(x) * np.sqrt(x), 2: lambda x: 1 / np.sqrt(1 - x * x),
+          3: lambda x: np.cos(50 * x) * np.exp(-x), 4: lambda x: np.exp(-x * x)}
+    for which, (a, b) in ((0, (0, 1)), (1, (0, 1)), (2, (-1, 1)), (3, (0, 3)), (4, (-2, 5))):
+        for er in (1e-4, 1e-8):
+            r, ier = oracle.qags_test(which, a, b, 1.49e-8, er)
+            assert r == quad(fs[which], a, b, epsrel=er)[0], (which, er)
+
+
+def test_halfbouncepath_matches_reference(oracle):
+    """flutils.halfbouncepath: field-line trace (RKF45), quadratic spline,
+    brentq and QAGS, against the reference's values (equatorial cases included)."""
+    for mid, L, pa, phi, Bm, Sb in GOLD["bounce_halfpath"]:
+        f = oracle.field(int(mid))
+        tpos = [0, L * Re * np.cos(np.radians(phi)), L * Re * np.sin(np.radians(phi)), 0.0]
+        got, n = oracle.halfbouncepath(f, tpos, Bm)
+        assert abs(got - Sb) <= 1e-11 * Sb, (mid, L, pa, got, Sb)
+
+
+def test_gc_bounceperiod_matches_reference(oracle):
+    f = oracle.field("DoubleDipole")
+    for row in GOLD["bounce_gc_period"]:
+        tr = oracle.gc_new_pa(f, row[0:3], row[3], row[4], 0.0, row[5], row[6])
+        assert abs(oracle.gc_bounceperiod(f, tr) - row[7]) <= 1e-11 * row[7]
+
+
+def test_gc_bounce_cadence_trajectory(oracle):
+    """GuidingCenter.advance with GCtimestep = 0: output rows every
+    bounceperiod / bounceresolution (GuidingCenter.py:443-446)."""
+    ref = GOLD["traj_gbounce_rows"]
+    init = GOLD["traj_gbounce_init"]
+    f = oracle.field("DoubleDipole")
+    c = oracle.config(rtol=1e-8, atol=1e-8, gctimestep=0.0)
+    tr = oracle.gc_new_pa(f, init[0:3], init[3], init[4], 0.0, init[5], init[6])
+    raised, rows = oracle.advance(f, c, tr, 0.5)
+    assert rows.shape[0] == ref.shape[0] - 1
+    # the cadence agrees to ~1e-13; positions relative to |r| (z crosses zero)
+    assert np.allclose(rows[:, 0], ref[1:, 0], rtol=1e-12, atol=0)
+    dpos = np.linalg.norm(rows[:, 1:4] - ref[1:, 1:4], axis=1) / np.linalg.norm(ref[1:, 1:4], axis=1)
+    assert dpos.max() < 1e-11 and np.allclose(rows[:, 4], ref[1:, 4], rtol=1e-10, atol=0)
+    cnt = GOLD["traj_gbounce_counters"]
+    assert (tr.nfcn, tr.nstep, tr.naccept, tr.nreject) == tuple(cnt.sum(axis=0))
