@@ -67,9 +67,10 @@ enum {
   RAPT_ST_NONFINITE = 4,      /* NaN/Inf in the state */
   RAPT_ST_GC_NOCONV = 5,      /* utils.guidingcenter did not converge (reference returns None) */
   RAPT_ST_ROWS_FULL = 6,      /* output row buffer full: drain rows and call again to resume */
-  RAPT_ST_BAD_INPUT = 7,      /* e.g. GCtimestep == 0 (bounce-period cadence not on device) */
+  RAPT_ST_BAD_INPUT = 7,      /* e.g. a GC cadence that is not > 0 */
   RAPT_ST_RKF_HMIN = 8,       /* rkf.py RuntimeError at hmin */
-  RAPT_ST_ADAPTIVE_LIMIT = 9  /* adaptive segment cap reached */
+  RAPT_ST_ADAPTIVE_LIMIT = 9, /* adaptive segment cap reached */
+  RAPT_ST_FIELDLINE = 10      /* bounce period: field-line trace longer than the device buffer, or no finite result */
 };
 
 /* Per-tracer flag bits (rapt_host_state.flags). */
@@ -83,7 +84,7 @@ enum {
 typedef struct {
   double rtol, atol;             /* params["solvertolerances"] */
   double cyclotronresolution;    /* params["cyclotronresolution"] */
-  double gctimestep;             /* params["GCtimestep"], must be > 0 */
+  double gctimestep;             /* params["GCtimestep"]; 0: bounce-period cadence */
   double epss, epst;             /* params["epss"], params["epst"] */
   int32_t enforce_equatorial;    /* params["enforce equatorial"] */
   int32_t tableau;               /* 0: DOP853 particle / DOPRI5 GC (as the reference); 1: RKF45 (rkf.py) */
@@ -103,6 +104,9 @@ typedef struct {
                                     correction in between (0 or 1: every step) */
   int32_t per_tracer_launches;   /* 1: one launch sequence per tracer (the unbatched pattern, for
                                     comparison); 0: one persistent grid for the whole ensemble */
+  double bounceresolution;       /* params["bounceresolution"]: with gctimestep == 0 the GC cadence is
+                                    bounceperiod() / bounceresolution (GuidingCenter.py:443-446) */
+  double fieldlineresolution;    /* params["fieldlineresolution"] (fieldline.py:31-35) */
 } rapt_config;
 
 /* Host-side SoA view of an ensemble. Any pointer may be NULL on download to
@@ -191,6 +195,13 @@ int rapt_field_eval(void* ctx, int what, int64_t n, const double* tpos, double* 
  * mass/charge/v; out[n][6]. */
 int rapt_rhs_eval(void* ctx, int mode, int64_t n, const double* state, const double* mass,
                   const double* charge, const double* v, double* out);
+
+/* GuidingCenter.bounceperiod (GuidingCenter.py:593-606; field-line trace and
+ * flutils.halfbouncepath, flutils.py:254-316) for n states, one GPU thread each:
+ * state[n][7] = (t, x, y, z, ppar, mu, mass) host, out[n] host (s); NaN where
+ * the trace exceeds the device buffer (1024 points per direction). Uses the
+ * config's fieldlineresolution. */
+int rapt_gc_bounce_period(void* ctx, int64_t n, const double* state, double* out);
 
 /* --- allocation-free guiding-centre advance ------------------------------- */
 /* No counterpart in the reference: RAPT has no device code and no notion of

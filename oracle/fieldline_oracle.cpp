@@ -107,7 +107,9 @@ void trace_sB(const orc_field* f, const double* tpos, double Bm, double flres, s
     const double sign = dir == 0 ? 1.0 : -1.0;
     for (long guard = 0; guard < 10000000; ++guard) {
       const double last[4] = {c[c.size() - 4], c[c.size() - 3], c[c.size() - 2], c[c.size() - 1]};
-      if (!rkf_segment(f, tpos[0], sign, last, ds, tol, ds, 1e-6, c)) break;
+      // rkf raising: the reference keeps none of that call's points (fieldline.py:68-69)
+      const size_t before = c.size();
+      if (!rkf_segment(f, tpos[0], sign, last, ds, tol, ds, 1e-6, c)) { c.resize(before); break; }
       const double tp[4] = {tpos[0], c[c.size() - 3], c[c.size() - 2], c[c.size() - 1]};
       if (orc_magB(f, tp) > Bm) break;
     }
@@ -621,6 +623,60 @@ L140:
   return result;
 }
 
+// Gauss-Legendre nodes and weights of order 8 by Newton's method on P_8.
+void gauss_legendre8(double* x, double* w) {
+  const int n = 8;
+  for (int i = 0; i < n / 2; ++i) {
+    double z = std::cos(kPiF * (i + 0.75) / (n + 0.5)), pp = 0.0;
+    for (int it = 0; it < 100; ++it) {
+      double p1 = 1.0, p2 = 0.0;
+      for (int j = 1; j <= n; ++j) {
+        const double p3 = p2;
+        p2 = p1;
+        p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+      }
+      pp = n * (z * p1 - p2) / (z * z - 1.0);
+      const double z1 = z;
+      z = z1 - p1 / pp;
+      if (std::fabs(z - z1) <= 1e-16) break;
+    }
+    x[i] = -z;
+    x[n - 1 - i] = z;
+    w[i] = w[n - 1 - i] = 2.0 / ((1.0 - z * z) * pp * pp);
+  }
+}
+
+// The half-bounce integral of the spline to convergence (the device's method):
+// s = c + h sin(theta) removes the inverse-square-root singularities at the
+// mirror points, and an 8-point Gauss-Legendre rule runs on every panel between
+// the images of the spline's knots (each panel a smooth polynomial piece).
+double bounce_integral_converged(const Spline2& sp, double sm1, double sm2, double Bm) {
+  double gx[8], gw[8];
+  gauss_legendre8(gx, gw);
+  const double c = 0.5 * (sm1 + sm2), h = 0.5 * (sm2 - sm1);
+  double sum = 0.0, ea = -kPiF / 2;
+  for (int j = 3; j <= sp.n; ++j) {
+    double eb;
+    if (j < sp.n) {
+      const double tj = sp.t[j];
+      if (!(tj > sm1 && tj < sm2)) continue;
+      eb = std::asin((tj - c) / h);
+    } else {
+      eb = kPiF / 2;
+    }
+    const double mid = 0.5 * (ea + eb), half = 0.5 * (eb - ea);
+    double ps = 0.0;
+    for (int k = 0; k < 8; ++k) {
+      const double th = mid + half * gx[k];
+      const double arg = 1.0 - sp(c + h * std::sin(th)) / Bm;
+      if (arg > 0.0) ps += gw[k] * (h * std::cos(th) / std::sqrt(arg));
+    }
+    sum += half * ps;
+    ea = eb;
+  }
+  return sum;
+}
+
 }  // namespace
 
 extern "C" {
@@ -651,7 +707,7 @@ int orc_fieldline_sB(const orc_field* f, const double* tpos, double Bm, double f
   return n;
 }
 
-double orc_halfbouncepath(const orc_field* f, const double* tpos, double Bm, double flres, int* npts) {
+double orc_halfbouncepath(const orc_field* f, const double* tpos, double Bm, double flres, int quad, int* npts) {
   // flutils.halfbouncepath, rapt/flutils.py:254-316
   std::vector<double> s, b;
   trace_sB(f, tpos, Bm, flres, s, b);
@@ -687,11 +743,12 @@ double orc_halfbouncepath(const orc_field* f, const double* tpos, double Bm, dou
   const double xtol = 2e-12, rtol = 4 * DBL_EPSILON;
   const double sm1 = brentq(g, ss[0], ss[1], xtol, rtol, 100);
   const double sm2 = brentq(g, ss[n - 2], ss[n - 1], xtol, rtol, 100);
+  if (quad == 1) return bounce_integral_converged(sp, sm1, sm2, Bm);
   int ier = 0;
   return qags([&](double x) { return 1 / std::sqrt(1 - sp(x) / Bm); }, sm1, sm2, 1.49e-8, 1e-4, 50, ier);
 }
 
-double orc_gc_bounceperiod(const orc_field* f, const orc_tracer* g, double flres) {
+double orc_gc_bounceperiod(const orc_field* f, const orc_tracer* g, double flres, int quad) {
   // GuidingCenter.bounceperiod, rapt/GuidingCenter.py:593-606 (state = trajectory[-1])
   const double c = 299792458.0;
   const double tpos[4] = {g->t, g->s[0], g->s[1], g->s[2]};
@@ -708,7 +765,7 @@ double orc_gc_bounceperiod(const orc_field* f, const orc_tracer* g, double flres
     Bmirror = p * p / ((p - ppar) * (p + ppar)) * Bmag;
     v = p / m / gamma;
   }
-  return (2 / v) * orc_halfbouncepath(f, tpos, Bmirror, flres, nullptr);
+  return (2 / v) * orc_halfbouncepath(f, tpos, Bmirror, flres, quad, nullptr);
 }
 
 }  // extern "C"

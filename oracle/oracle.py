@@ -38,7 +38,7 @@ class Config(C.Structure):
                 ("gctimestep", C.c_double), ("epss", C.c_double), ("epst", C.c_double),
                 ("enforce_equatorial", C.c_int), ("tableau", C.c_int), ("gc_eom", C.c_int),
                 ("nsteps", C.c_int), ("rkf_tol", C.c_double), ("rkf_hmin", C.c_double),
-                ("bounceres", C.c_double), ("flres", C.c_double)]
+                ("bounceres", C.c_double), ("flres", C.c_double), ("bounce_quad", C.c_int)]
 
 
 TRACER_DTYPE = np.dtype([
@@ -103,8 +103,8 @@ def lib():
                                                _P(C.c_int), _dp, _P(C.c_int8), C.c_int,
                                                _P(C.c_int)]),
             "orc_batch_advance": (None, [F, Cf, C.c_int, C.c_int64, C.c_void_p, _dp, C.c_int]),
-            "orc_gc_bounceperiod": (_d, [F, T, _d]),
-            "orc_halfbouncepath": (_d, [F, _dp, _d, _d, _P(C.c_int)]),
+            "orc_gc_bounceperiod": (_d, [F, T, _d, C.c_int]),
+            "orc_halfbouncepath": (_d, [F, _dp, _d, _d, C.c_int, _P(C.c_int)]),
             "orc_fieldline_sB": (C.c_int, [F, _dp, _d, _d, _dp, _dp, C.c_int]),
             "orc_qags_test": (_d, [C.c_int, _d, _d, _d, _d, C.c_int, _P(C.c_int)]),
         }
@@ -134,10 +134,10 @@ def field(name_or_id, params=()):
 
 def config(rtol=1.49012e-8, atol=1.49012e-8, cycres=10, gctimestep=0.0, epss=5e-2, epst=5e-2,
            enforce_equatorial=False, tableau=0, gc_eom=0, nsteps=500, rkf_tol=1e-3,
-           rkf_hmin=1e-12, bounceres=10, flres=50):
+           rkf_hmin=1e-12, bounceres=10, flres=50, bounce_quad=0):
     c = Config()
     lib().orc_config_default(C.byref(c))
-    c.bounceres, c.flres = bounceres, flres
+    c.bounceres, c.flres, c.bounce_quad = bounceres, flres, bounce_quad
     c.rtol, c.atol, c.cycres, c.gctimestep = rtol, atol, cycres, gctimestep
     c.epss, c.epst, c.enforce_equatorial = epss, epst, int(bool(enforce_equatorial))
     c.tableau, c.gc_eom, c.nsteps, c.rkf_tol, c.rkf_hmin = tableau, gc_eom, nsteps, rkf_tol, rkf_hmin
@@ -239,16 +239,17 @@ def tracers_from_structs(structs):
     return arr
 
 
-def halfbouncepath(f, tpos, Bm, flres=50.0):
-    """flutils.halfbouncepath (rapt/flutils.py:254-316); returns (S_b, points kept)."""
+def halfbouncepath(f, tpos, Bm, flres=50.0, quad=0):
+    """flutils.halfbouncepath (rapt/flutils.py:254-316); returns (S_b, points kept).
+    quad 0: QAGS as the reference; 1: the converged integral of the same spline."""
     t, tp = _vec(tpos, 4)
     n = C.c_int(0)
-    return lib().orc_halfbouncepath(C.byref(f), tp, float(Bm), float(flres), C.byref(n)), n.value
+    return lib().orc_halfbouncepath(C.byref(f), tp, float(Bm), float(flres), int(quad), C.byref(n)), n.value
 
 
-def gc_bounceperiod(f, tr, flres=50.0):
+def gc_bounceperiod(f, tr, flres=50.0, quad=0):
     """GuidingCenter.bounceperiod (rapt/GuidingCenter.py:593-606) of a GC tracer struct."""
-    return lib().orc_gc_bounceperiod(C.byref(f), C.byref(tr), float(flres))
+    return lib().orc_gc_bounceperiod(C.byref(f), C.byref(tr), float(flres), int(quad))
 
 
 def fieldline_sB(f, tpos, Bm, flres=50.0, cap=100000):

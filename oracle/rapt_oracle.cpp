@@ -59,6 +59,7 @@ void orc_config_default(orc_config* c) {
   c->nsteps = 500;
   c->bounceres = 10;
   c->flres = 50;
+  c->bounce_quad = 0;
   c->rkf_tol = 1e-3;
   c->rkf_hmin = 1e-12;
 }
@@ -957,7 +958,7 @@ int orc_gc_advance(const orc_field* f, const orc_config* c, orc_tracer* g, doubl
                    int check_adiabaticity, double* rows, int max_rows, int* nrows) {
   // GuidingCenter.advance, rapt/GuidingCenter.py:397-458 (dopri5 at :450)
   // cadence: GCtimestep, or the bounce period at the current state / bounceresolution (:443-446)
-  const double dt = c->gctimestep != 0 ? c->gctimestep : orc_gc_bounceperiod(f, g, c->flres) / c->bounceres;
+  const double dt = c->gctimestep != 0 ? c->gctimestep : orc_gc_bounceperiod(f, g, c->flres, c->bounce_quad) / c->bounceres;
   if (!(dt > 0) || !std::isfinite(dt)) { g->status = ORC_ST_BAD_INPUT; return 0; }
   const double t0 = g->t;
   double rt = g->t;

@@ -50,6 +50,7 @@ typedef struct {
   double rkf_tol, rkf_hmin;/* RKF45 tableau: rkf.py tol and hmin */
   double bounceres;        /* params["bounceresolution"]: GC cadence T_b / bounceres when gctimestep == 0 */
   double flres;            /* params["fieldlineresolution"] */
+  int bounce_quad;         /* half-bounce integral: 0 QAGS as the reference, 1 converged */
 } orc_config;
 
 /* One tracer (a Particle or a GuidingCenter segment). */
@@ -127,9 +128,11 @@ int orc_gc_advance(const orc_field* f, const orc_config* c, orc_tracer* g, doubl
 /* Field lines and the bounce period (fieldline_oracle.cpp): GuidingCenter.bounceperiod
  * (GuidingCenter.py:593-606), flutils.halfbouncepath (flutils.py:254-316), the
  * (s, |B|) samples of Fieldline.trace (fieldline.py:37-107), and QAGS on test
- * integrands (for pinning against scipy.integrate.quad). */
-double orc_gc_bounceperiod(const orc_field* f, const orc_tracer* g, double flres);
-double orc_halfbouncepath(const orc_field* f, const double* tpos, double Bm, double flres, int* npts);
+ * integrands (for pinning against scipy.integrate.quad). quad 0: the half-bounce
+ * integral by QAGS at epsrel 1e-4 as the reference; 1: converged (substitution
+ * and composite Gauss-Legendre, the device's method). */
+double orc_gc_bounceperiod(const orc_field* f, const orc_tracer* g, double flres, int quad);
+double orc_halfbouncepath(const orc_field* f, const double* tpos, double Bm, double flres, int quad, int* npts);
 int orc_fieldline_sB(const orc_field* f, const double* tpos, double Bm, double flres, double* s, double* B,
                      int cap);
 double orc_qags_test(int which, double a, double b, double epsabs, double epsrel, int limit, int* ier);

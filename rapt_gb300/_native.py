@@ -18,7 +18,7 @@ MODEL_IDS = {"EarthDipole": 0, "DoubleDipole": 1, "UniformBz": 2, "UniformCrosse
 MODE_PARTICLE, MODE_GC = 0, 1
 KIND_PARTICLE, KIND_GC, KIND_ADAPTIVE = 0, 1, 2
 FORMS = {"plain": 0, "fp32": 1, "learned": 2, "learned_fp32": 3}
-ST = dict(OK=0, MAXSTEPS=2, HMIN=3, NONFINITE=4, GC_NOCONV=5, ROWS_FULL=6, BAD_INPUT=7,
+ST = dict(OK=0, MAXSTEPS=2, HMIN=3, NONFINITE=4, GC_NOCONV=5, ROWS_FULL=6, BAD_INPUT=7, FIELDLINE=10,
           RKF_HMIN=8, ADAPTIVE_LIMIT=9)
 FLAG_CHECK, FLAG_RAISED, FLAG_DONE = 1, 2, 4
 FIELD_QUANTITIES = {"B": 0, "E": 1, "gradB": 2, "curlb": 3, "magB": 4, "unitb": 5,
@@ -33,7 +33,8 @@ class RaptConfig(C.Structure):
                 ("form", C.c_int32), ("threads_per_block", C.c_int32),
                 ("max_steps_per_launch", C.c_int64), ("blocks_per_sm", C.c_int32),
                 ("use_graph", C.c_int32), ("collect", C.c_int32), ("learned_scale", C.c_double),
-                ("learned_every", C.c_int32), ("per_tracer_launches", C.c_int32)]
+                ("learned_every", C.c_int32), ("per_tracer_launches", C.c_int32),
+                ("bounceresolution", C.c_double), ("fieldlineresolution", C.c_double)]
 
 
 class RaptHostState(C.Structure):
@@ -79,6 +80,7 @@ SIGNATURES = {
     "rapt_host_unregister": (C.c_int, [_VP]),
     "rapt_gc_advance_noalloc": (C.c_int, [C.c_int, C.c_int, _DP, C.c_int, C.POINTER(RaptConfig), _VP, _D, _VP,
                                           C.POINTER(RaptStats)]),
+    "rapt_gc_bounce_period": (C.c_int, [_VP, _I64, _VP, _VP]),
     "rapt_mlp_set_params": (C.c_int, [_VP, _VP, C.c_int32]),
     "rapt_mlp_get_params": (C.c_int, [_VP, _VP, C.c_int32]),
     "rapt_mlp_forward": (C.c_int, [_VP, _VP, _I64, _VP]),
@@ -201,6 +203,13 @@ class Context:
         out = np.zeros((n, 6))
         self.check(self.L.rapt_rhs_eval(self.h, int(mode), n, ptr(state), ptr(mass), ptr(charge), ptr(vv), ptr(out)),
                    "rapt_rhs_eval")
+        return out
+
+    def gc_bounce_period(self, state):
+        """Bounce periods of GC states [n][7] = (t, x, y, z, ppar, mu, mass)."""
+        st = np.ascontiguousarray(np.atleast_2d(state), dtype=np.float64)
+        out = np.zeros(st.shape[0])
+        self.check(self.L.rapt_gc_bounce_period(self.h, st.shape[0], ptr(st), ptr(out)), "rapt_gc_bounce_period")
         return out
 
     # ---- step-size MLP

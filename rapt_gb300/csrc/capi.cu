@@ -42,6 +42,8 @@ struct Ctx {
   uint32_t* mlp_w = nullptr;
   bool mlp_ready = false;
   int64_t mlp_t = 0;  // Adam step count
+  double* fl_scratch = nullptr;  // field-line traces of the bounce-period cadence
+  size_t fl_bytes = 0;
   float* samp = nullptr;
   unsigned long long* samp_count = nullptr;
   int64_t samp_cap = 0;
@@ -133,6 +135,10 @@ void finish_field(FieldP* f) {
   }
 }
 
+// trace points per direction of the bounce-period field-line trace; a thread's
+// scratch is 8 * kFieldlineCap doubles (64 KB)
+constexpr int kFieldlineCap = 1024;
+
 KParams make_params(const Ctx* c, int kind) {
   KParams P{};
   P.f = c->field;
@@ -152,6 +158,11 @@ KParams make_params(const Ctx* c, int kind) {
   P.samp_cap = c->samp_cap;
   P.samp_mask = c->samp_mask;
   P.collect = g.collect;
+  P.bounceres = g.bounceresolution;
+  P.flres = g.fieldlineresolution;
+  P.fl_scratch = nullptr;
+  P.fl_cap = kFieldlineCap;
+  P.fl_stride = 8LL * kFieldlineCap;
   P.learn_every = g.learned_every > 1 ? g.learned_every : 1;
   return P;
 }
@@ -209,6 +220,8 @@ void rapt_config_default(rapt_config* g) {
   g->nsteps = 500;
   g->rkf_tol = 1e-3;
   g->rkf_hmin = 1e-12;
+  g->bounceresolution = 10;
+  g->fieldlineresolution = 50;
 }
 
 int rapt_ctx_create(int device, void** out) {
@@ -248,6 +261,7 @@ void rapt_ctx_destroy(void* ctx) {
   cudaFree(c->scratch);
   cudaFree(c->tmp);
   cudaFree(c->mlp_block);
+  cudaFree(c->fl_scratch);
   cudaFree(c->samp_count);  // base of the sample allocation
   cudaFreeHost(c->h_pending);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -301,6 +315,9 @@ int rapt_config_set(void* ctx, const rapt_config* g) {
     return fail(c, RAPT_ERR_UNSUPPORTED, "the step learner drives the DOPRI5 controller (tableau 0)");
   if (!(g->learned_scale >= 0)) return fail(c, RAPT_ERR_INVALID, "learned_scale must be >= 0");
   if (g->learned_every < 0) return fail(c, RAPT_ERR_INVALID, "learned_every must be >= 0");
+  if (!(g->gctimestep >= 0)) return fail(c, RAPT_ERR_INVALID, "GCtimestep must be >= 0");
+  if (g->gctimestep == 0 && !(g->bounceresolution > 0 && g->fieldlineresolution > 0))
+    return fail(c, RAPT_ERR_INVALID, "bounceresolution and fieldlineresolution must be > 0");
   c->cfg = *g;
   return RAPT_OK;
 }
@@ -504,7 +521,7 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
     d_delta = static_cast<double*>(c->tmp);
     CK(cudaMemcpyAsync(d_delta, delta, N * 8, cudaMemcpyHostToDevice, s));
   }
-  const KParams P = make_params(c, kind);
+  KParams P = make_params(c, kind);
   const ModelTable& T = c->tab[c->field.model];
   const int tab = c->cfg.tableau;
   const int block = c->cfg.threads_per_block > 0 ? c->cfg.threads_per_block : 128;
@@ -524,6 +541,22 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
     bps_g = std::min(bps_g, c->cfg.blocks_per_sm);
   }
   if (bps_p < 1 || bps_g < 1) return fail(c, RAPT_ERR_CUDA, "kernel does not fit on an SM");
+  if (kind != RAPT_KIND_PARTICLE && c->cfg.gctimestep == 0) {
+    // bounce-period cadence: one field-line scratch slot per guiding-centre thread
+    const size_t threads = c->cfg.per_tracer_launches ? 32 : (size_t)c->num_sms * bps_g * block;
+    const size_t bytes = threads * (size_t)P.fl_stride * sizeof(double);
+    if (c->fl_bytes < bytes) {
+      cudaFree(c->fl_scratch);
+      c->fl_scratch = nullptr;
+      c->fl_bytes = 0;
+      if (cudaMalloc(&c->fl_scratch, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, RAPT_ERR_NOMEM, "cudaMalloc(%zu bytes) for field-line traces failed", bytes);
+      }
+      c->fl_bytes = bytes;
+    }
+    P.fl_scratch = c->fl_scratch;
+  }
 
   CK(cudaEventRecord(c->ev0, s));
   if (resume) k_clear_rows_full<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(E);
@@ -878,6 +911,38 @@ int rapt_mlp_train(void* ctx, int64_t steps, int32_t batch, float lr, float swit
   CK(cudaMemcpyAsync(hl, c->mlp_loss, 16, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   if (loss) { loss[0] = hl[0] / (double)tail; loss[1] = hl[1] / (double)tail; }
+  return RAPT_OK;
+}
+
+int rapt_gc_bounce_period(void* ctx, int64_t n, const double* state, double* out) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || n < 0 || (n > 0 && (!state || !out))) return RAPT_ERR_INVALID;
+  if (!c->field_set) return fail(c, RAPT_ERR_STATE, "no field set");
+  if (n == 0) return RAPT_OK;
+  CK(cudaSetDevice(c->device));
+  const size_t N = (size_t)n;
+  const long long stride = 8LL * kFieldlineCap;
+  int rc = ensure_tmp(c, N * 8 * 8);
+  if (rc) return rc;
+  double* d_in = static_cast<double*>(c->tmp);
+  double* d_out = d_in + 7 * N;
+  // scratch for the traces: reuse the advance buffer when it is large enough
+  const size_t need = N * (size_t)stride * sizeof(double);
+  if (c->fl_bytes < need) {
+    cudaFree(c->fl_scratch);
+    c->fl_scratch = nullptr;
+    c->fl_bytes = 0;
+    if (cudaMalloc(&c->fl_scratch, need) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(c, RAPT_ERR_NOMEM, "cudaMalloc(%zu bytes) for field-line traces failed", need);
+    }
+    c->fl_bytes = need;
+  }
+  CK(cudaMemcpyAsync(d_in, state, N * 7 * 8, cudaMemcpyHostToDevice, c->stream));
+  CK(c->tab[c->field.model].bounce_period(c->field, c->cfg.fieldlineresolution, n, d_in, d_out, c->fl_scratch,
+                                          stride, kFieldlineCap, c->stream));
+  CK(cudaMemcpyAsync(out, d_out, N * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   return RAPT_OK;
 }
 

@@ -48,6 +48,11 @@ struct KParams {
   unsigned long long samp_mask;  // an accepted step is sampled when its hash & mask == 0
   int collect;             // learned kernels: also record samples (on-policy data)
   int learn_every;         // run the MLP on every k-th accepted step, reuse its correction between
+  // bounce-period cadence (gctimestep == 0): per-thread field-line scratch
+  double bounceres, flres; // params["bounceresolution"], params["fieldlineresolution"]
+  double* fl_scratch;      // fl_stride doubles per thread of the launch
+  long long fl_stride;
+  int fl_cap;              // trace points per direction
 };
 
 // Device SoA ensemble (all arrays length n unless noted).

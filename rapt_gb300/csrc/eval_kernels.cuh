@@ -89,4 +89,17 @@ __global__ void k_adaptive_init(DevEnsemble E, KParams P) {
   E.mode[k] = RAPT_MODE_GC;
 }
 
+// GuidingCenter.bounceperiod (GuidingCenter.py:593-606) for n states
+// (t, x, y, z, ppar, mu, mass); one thread each, fl_stride doubles of scratch
+// per thread. NaN where the trace does not fit the buffer.
+template <int M>
+__global__ void k_bounce_period(FieldP f, double flres, int64_t n, const double* in, double* out, double* scratch,
+                                long long stride, int cap) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double* r = in + 7 * k;
+  const double y[4] = {r[1], r[2], r[3], r[4]};
+  out[k] = gc_bounceperiod<M>(f, r[0], y, r[5], r[6], flres, scratch + (size_t)k * (size_t)stride, cap);
+}
+
 }  // namespace rapt

@@ -274,7 +274,14 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
     dt = P.gctimestep;
     stop = t_row + seg_delta;
     seg_ok = true;
-    if (!(dt > 0.0)) { seg_ok = false; status = RAPT_ST_BAD_INPUT; }
+    if (dt == 0.0 && P.fl_scratch) {  // bounce-period cadence (GuidingCenter.py:443-446)
+      double s4[6];
+      state_si(s4);
+      double* scr = P.fl_scratch + (size_t)(blockIdx.x * blockDim.x + threadIdx.x) * (size_t)P.fl_stride;
+      dt = gc_bounceperiod<M>(P.f, t_row, s4, mu, mass, P.flres, scr, P.fl_cap) / P.bounceres;
+      if (!(dt > 0.0) || !isfinite(dt)) { seg_ok = false; status = RAPT_ST_FIELDLINE; dt = 0.0; }
+    }
+    if (!(dt > 0.0) && status != RAPT_ST_FIELDLINE) { seg_ok = false; status = RAPT_ST_BAD_INPUT; }
     k1_valid = false;
     in_interval = false;
   };

@@ -91,6 +91,12 @@ cudaError_t rhs_eval(const KParams& P, int mode, int64_t n, const double* state,
   k_rhs_eval<kM><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(P, mode, n, state, mass, charge, v, out);
   return cudaGetLastError();
 }
+cudaError_t bounce_period(const FieldP& f, double flres, int64_t n, const double* in, double* out, double* scratch,
+                          long long stride, int cap, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_bounce_period<kM><<<(unsigned)((n + 63) / 64), 64, 0, s>>>(f, flres, n, in, out, scratch, stride, cap);
+  return cudaGetLastError();
+}
 cudaError_t adaptive_init(const DevEnsemble& E, const KParams& P, cudaStream_t s) {
   if (E.n <= 0) return cudaSuccess;
   k_adaptive_init<kM><<<(unsigned)((E.n + 127) / 128), 128, 0, s>>>(E, P);
@@ -126,5 +132,6 @@ void RAPT_CAT(register_model_, RAPT_MODEL)(ModelTable* t) {
   t->field_eval = field_eval;
   t->rhs_eval = rhs_eval;
   t->adaptive_init = adaptive_init;
+  t->bounce_period = bounce_period;
 }
 }  // namespace rapt

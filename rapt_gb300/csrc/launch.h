@@ -20,6 +20,8 @@ using FieldEvalFn = cudaError_t (*)(const FieldP& f, int what, int64_t n, const 
 using RhsEvalFn = cudaError_t (*)(const KParams& P, int mode, int64_t n, const double* state, const double* mass,
                                   const double* charge, const double* v, double* out, cudaStream_t s);
 using AdaptiveInitFn = cudaError_t (*)(const DevEnsemble& E, const KParams& P, cudaStream_t s);
+using BounceFn = cudaError_t (*)(const FieldP& f, double flres, int64_t n, const double* in, double* out,
+                                 double* scratch, long long stride, int cap, cudaStream_t s);
 
 struct ModelTable {
   LaunchFn particle[2];  // [tableau]
@@ -35,6 +37,7 @@ struct ModelTable {
   FieldEvalFn field_eval;
   RhsEvalFn rhs_eval;
   AdaptiveInitFn adaptive_init;
+  BounceFn bounce_period;
 };
 
 // MLP kernels (mlp.cu); packed BF16 weights take kMlpPackedWords u32

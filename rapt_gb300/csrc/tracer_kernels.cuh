@@ -19,6 +19,7 @@
 // each output row. Every loop is bounded: nsteps per interval, the per-launch
 // step budget, 20 guiding-centre iterations, and the Adaptive segment cap.
 #pragma once
+#include "fieldline.cuh"
 #include "mlp.cuh"
 #include "rhs.cuh"
 #include "steppers.cuh"
@@ -546,7 +547,12 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
     dt = P.gctimestep;
     stop = t_row + seg_delta;
     seg_ok = true;
-    if (!(dt > 0.0)) { seg_ok = false; status = RAPT_ST_BAD_INPUT; }
+    if (dt == 0.0 && P.fl_scratch) {  // bounce-period cadence
+      double* scr = P.fl_scratch + (size_t)(blockIdx.x * blockDim.x + threadIdx.x) * (size_t)P.fl_stride;
+      dt = gc_bounceperiod<M>(P.f, t_row, y, mu, mass, P.flres, scr, P.fl_cap) / P.bounceres;
+      if (!(dt > 0.0) || !isfinite(dt)) { seg_ok = false; status = RAPT_ST_FIELDLINE; dt = 0.0; }
+    }
+    if (!(dt > 0.0) && status != RAPT_ST_FIELDLINE) { seg_ok = false; status = RAPT_ST_BAD_INPUT; }
     k1_valid = false;
     in_interval = false;
   };

@@ -34,7 +34,8 @@ def _config(eom=0, tableau=0):
     rtol, atol = p["solvertolerances"]
     return dict(rtol=rtol, atol=atol, cyclotronresolution=p["cyclotronresolution"], gctimestep=p["GCtimestep"],
                 epss=p["epss"], epst=p["epst"], enforce_equatorial=int(bool(p["enforce equatorial"])),
-                gc_eom=eom, tableau=tableau)
+                gc_eom=eom, tableau=tableau, bounceresolution=p["bounceresolution"],
+                fieldlineresolution=p["fieldlineresolution"])
 
 
 class _Pickle:
@@ -281,8 +282,14 @@ class GuidingCenter(_Pickle):
             raise NonAdiabatic
 
     def bounceperiod(self):
-        raise NotImplementedError("bounce period needs field-line tracing, which has no device implementation; "
-                                  "set params['GCtimestep'] > 0")
+        """GuidingCenter.bounceperiod (GuidingCenter.py:593-606) at the current
+        state: field-line trace and half-bounce path on the GPU."""
+        from . import _native
+        ctx = _native.default_context()
+        self.field.bind(ctx)
+        ctx.set_config(**_config())
+        row = self.trajectory[-1]
+        return float(ctx.gc_bounce_period(np.r_[row[0:5], self.mu, self.mass])[0])
 
     def geteye(self, step=1):
         raise NotImplementedError("second invariant (field-line integrals) has no device implementation")
@@ -428,9 +435,6 @@ def advance_batch(tracers, delta, eom="TaoChanBrizardEOM", tableau=0, verbose=Fa
     if any(type(t) is not cls or t.field is not field for t in tracers):
         raise ValueError("advance_batch needs tracers of one class sharing one field object")
     kind = {Particle: N.KIND_PARTICLE, GuidingCenter: N.KIND_GC, Adaptive: N.KIND_ADAPTIVE}[cls]
-    if kind != N.KIND_PARTICLE and not (_params()["GCtimestep"] > 0):
-        raise NotImplementedError("GCtimestep = 0 selects the bounce-period cadence, which needs field-line "
-                                  "tracing (no device implementation); set params['GCtimestep'] > 0")
     n = len(tracers)
     delta = np.broadcast_to(np.asarray(delta, float), (n,)).copy()
     max_rows = _estimate_rows(kind, tracers, delta)

@@ -24,7 +24,7 @@ def oracle_config(O, w, **over):
                     epss=p.get("epss", 5e-2), epst=p.get("epst", 5e-2), tableau=p.get("tableau", 0),
                     gc_eom=p.get("gc_eom", 0), nsteps=p.get("nsteps", 500),
                     rkf_tol=p.get("rkf_tol", 1e-3), rkf_hmin=p.get("rkf_hmin", 1e-12),
-                    enforce_equatorial=p.get("enforce_equatorial", 0))
+                    enforce_equatorial=p.get("enforce_equatorial", 0), bounce_quad=p.get("bounce_quad", 0))
 
 
 def oracle_tracers(O, w, kind):

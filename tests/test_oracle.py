@@ -228,3 +228,13 @@ def test_gc_bounce_cadence_trajectory(oracle):
     assert dpos.max() < 1e-11 and np.allclose(rows[:, 4], ref[1:, 4], rtol=1e-10, atol=0)
     cnt = GOLD["traj_gbounce_counters"]
     assert (tr.nfcn, tr.nstep, tr.naccept, tr.nreject) == tuple(cnt.sum(axis=0))
+
+
+def test_converged_halfbounce_integral(oracle):
+    """The converged integral of the same spline (the device's method) differs
+    from the reference's QAGS (epsrel 1e-4) by that QAGS's own error."""
+    for mid, L, pa, phi, Bm, Sb in GOLD["bounce_halfpath"]:
+        f = oracle.field(int(mid))
+        tpos = [0, L * Re * np.cos(np.radians(phi)), L * Re * np.sin(np.radians(phi)), 0.0]
+        got, n = oracle.halfbouncepath(f, tpos, Bm, quad=1)
+        assert abs(got - Sb) <= 1e-5 * Sb, (mid, L, pa, got, Sb)
