@@ -102,7 +102,9 @@ def test_fields_without_device_implementation_raise(params):
     p = R.Particle([6 * R.Re, 0, 0], [0, 1e6, 0], 0, R.m_pr, R.e, MyField())
     with pytest.raises(NotImplementedError):
         p.advance(1.0)
+    # GCtimestep = 0 selects the bounce-period cadence, which runs on the device
     params.update(GCtimestep=0)
     g = R.GuidingCenter([5 * R.Re, 0, 0], 1e7, pa=45, mass=R.m_el, charge=-R.e, field=R.fields.DoubleDipole())
-    with pytest.raises(NotImplementedError):
-        g.advance(1.0)
+    tb = g.bounceperiod()
+    g.advance(0.3 * tb)
+    assert np.allclose(np.diff(g.trajectory[:, 0]), tb / 10, rtol=1e-9)
