@@ -44,7 +44,8 @@ enum {
   RAPT_PARABOLIC = 5,          /* Parabolic(B0, Bn, d)            fields.py:472-511 */
   RAPT_HARRIS = 6,             /* Harris sheet (B0, L, Bn, Ey): no reference counterpart */
   RAPT_COMPRESSED_DIPOLE = 7,  /* breathing dipole + induced E (B0, amp, period): no counterpart */
-  RAPT_N_MODELS = 8
+  RAPT_GRID = 8,               /* Grid(filelist): gridded snapshots   fields.py:513-814 (rapt_grid_set) */
+  RAPT_N_MODELS = 9
 };
 
 /* Tracer modes and run kinds. */
@@ -70,7 +71,9 @@ enum {
   RAPT_ST_BAD_INPUT = 7,      /* e.g. a GC cadence that is not > 0 */
   RAPT_ST_RKF_HMIN = 8,       /* rkf.py RuntimeError at hmin */
   RAPT_ST_ADAPTIVE_LIMIT = 9, /* adaptive segment cap reached */
-  RAPT_ST_FIELDLINE = 10      /* bounce period: field-line trace longer than the device buffer, or no finite result */
+  RAPT_ST_FIELDLINE = 10,     /* bounce period: field-line trace longer than the device buffer, or no finite result */
+  RAPT_ST_OUT_OF_GRID = 11    /* RAPT_GRID: a step evaluated the field outside the grid (the reference's
+                                 RegularGridInterpolator raises ValueError); the state is the last accepted one */
 };
 
 /* Per-tracer flag bits (rapt_host_state.flags). */
@@ -150,6 +153,24 @@ int rapt_field_set(void* ctx, int model, const double* params, int nparams);
 /* Stand-in for assigning field.gradientstepsize / field.timederivstepsize
  * (fields.py:38-41); call after rapt_field_set. */
 int rapt_field_set_steps(void* ctx, double gradientstepsize, double timederivstepsize);
+/* Stand-in for assigning field.static (fields.py:41). The analytic models'
+ * static-ness follows from their equations and ignores it; RAPT_GRID honours it
+ * (Grid leaves static = True, fields.py:41 via :577, even for time-dependent data). */
+int rapt_field_set_static(void* ctx, int is_static);
+/* Grid (fields.py:513-814): field snapshots at times t[nt] (strictly ascending)
+ * on the rectilinear axes x[nx], y[ny], z[nz] (strictly ascending, >= 2 points,
+ * spacing free). B and E are [nt][nx][ny][nz][3] float64 (component fastest);
+ * E may be NULL (zero electric field). nt == 1 is the time-independent case
+ * (3-D interpolation); nt >= 2 interpolates linearly in time between adjacent
+ * snapshots. Every snapshot stays resident on the device: the reference's
+ * three-snapshot sliding window (fields.py:695-705, :733-734) gives the same values on
+ * the interval it covers. Interpolation is SciPy's RegularGridInterpolator,
+ * method "linear" (corners in itertools.product order, FP64, no FMA), so values
+ * agree bit for bit. Selects RAPT_GRID as the field, gradientstepsize 1e-3 Re
+ * (fields.py:578), timederivstepsize 1e-3, static = 1. A later
+ * rapt_field_set(ctx, RAPT_GRID, NULL, 0) re-selects the resident grid. */
+int rapt_grid_set(void* ctx, int32_t nt, const double* t, int32_t nx, const double* x, int32_t ny,
+                  const double* y, int32_t nz, const double* z, const double* B, const double* E);
 /* Stand-in for rapt.params (rapt/__init__.py:21-34). */
 void rapt_config_default(rapt_config* cfg);
 int rapt_config_set(void* ctx, const rapt_config* cfg);

@@ -21,16 +21,19 @@ LIB_PATH = os.path.join(HERE, "librapt_oracle.so")
 
 FIELD_IDS = {
     "EarthDipole": 0, "DoubleDipole": 1, "UniformBz": 2, "UniformCrossedEB": 3,
-    "VarEarthDipole": 4, "Parabolic": 5, "Harris": 6, "CompressedDipole": 7,
+    "VarEarthDipole": 4, "Parabolic": 5, "Harris": 6, "CompressedDipole": 7, "Grid": 8,
 }
 
 ST = dict(OK=0, MAXSTEPS=2, HMIN=3, NONFINITE=4, GC_NOCONV=5, ROWS_FULL=6, BAD_INPUT=7,
-          RKF_HMIN=8, ADAPTIVE_LIMIT=9)
+          RKF_HMIN=8, ADAPTIVE_LIMIT=9, FIELDLINE=10, OUT_OF_GRID=11)
 
 
 class Field(C.Structure):
     _fields_ = [("model", C.c_int), ("is_static", C.c_int), ("p", C.c_double * 8),
-                ("gradstep", C.c_double), ("timestep", C.c_double)]
+                ("gradstep", C.c_double), ("timestep", C.c_double),
+                ("gt", C.POINTER(C.c_double)), ("gx", C.POINTER(C.c_double)), ("gy", C.POINTER(C.c_double)),
+                ("gz", C.POINTER(C.c_double)), ("gB", C.POINTER(C.c_double)), ("gE", C.POINTER(C.c_double)),
+                ("nt", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int)]
 
 
 class Config(C.Structure):
@@ -129,6 +132,23 @@ def field(name_or_id, params=()):
     f = Field()
     p = np.ascontiguousarray(params, dtype=np.float64)
     lib().orc_field_init(C.byref(f), mid, p.ctypes.data_as(_dp), len(p))
+    return f
+
+
+def grid_field(t, x, y, z, B, E=None, static=True):
+    """Oracle Grid field (rapt/fields.py:513-814) over snapshots at times t on the
+    axes x, y, z; B, E: [nt][nx][ny][nz][3]. The struct keeps the arrays alive."""
+    f = field("Grid")
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (t, x, y, z, B)]
+    arrs.append(None if E is None else np.ascontiguousarray(E, dtype=np.float64))
+    nt, nx, ny, nz = (len(a) for a in arrs[:4])
+    for a in arrs[4:]:
+        assert a is None or a.shape == (nt, nx, ny, nz, 3), a.shape
+    f._keep = arrs
+    f.gt, f.gx, f.gy, f.gz, f.gB = (a.ctypes.data_as(_dp) for a in arrs[:5])
+    f.gE = arrs[5].ctypes.data_as(_dp) if arrs[5] is not None else None
+    f.nt, f.nx, f.ny, f.nz = nt, nx, ny, nz
+    f.is_static = 1 if static else 0
     return f
 
 

@@ -104,12 +104,72 @@ void orc_field_init(orc_field* f, int model, const double* params, int nparams) 
       f->gradstep = kRe / 1000;
       f->is_static = 0;
       break;
+    case ORC_GRID:  // fields.py:577-578; the data are attached by the caller
+      f->gradstep = 1e-3 * kRe;
+      break;
     default:
       break;
   }
   for (int i = 0; i < nparams && i < 8; ++i) p[i] = params[i];
   if (model == ORC_HARRIS) f->gradstep = p[1] * 1e-4;
 }
+
+// ---------------------------------------------------------------- Grid
+// Grid.Bgrid / Egrid (rapt/fields.py:707-771) evaluate SciPy's
+// RegularGridInterpolator (method "linear", bounds_error=True) over
+// (t, x, y, z), or (x, y, z) for one snapshot. Restated from SciPy 1.18
+// interpolate/_rgi.py: _prepare_xi (bounds check: ValueError unless
+// g[0] <= v <= g[-1] on every axis), find_indices (the cell i with
+// g[i] <= v < g[i+1], the last cell for v == g[-1]; w = (v - g[i]) /
+// (g[i+1] - g[i])) and _evaluate_linear (corners in itertools.product order,
+// lower weight 1 - w, upper w; weight = ((1 * w_0) * w_1) ...; value summed from
+// 0 corner by corner). The reference's three-snapshot window (fields.py:695-705)
+// gives the same values as one interpolator over all snapshots on the interval
+// it covers. Outside the grid this returns NaN (the reference raises).
+namespace {
+bool grid_inside(const double* g, int n, double v) { return g[0] <= v && v <= g[n - 1]; }
+
+int grid_cell(const double* g, int n, double v, double* w) {
+  int i = 0;
+  while (i + 2 < n && g[i + 1] <= v) ++i;  // linear scan: the oracle favours plainness
+  *w = (v - g[i]) / (g[i + 1] - g[i]);
+  return i;
+}
+
+void grid_eval(const orc_field* f, const double* V, const double* tpos, double* o) {
+  const double t = tpos[0], x = tpos[1], y = tpos[2], z = tpos[3];
+  if (!grid_inside(f->gx, f->nx, x) || !grid_inside(f->gy, f->ny, y) || !grid_inside(f->gz, f->nz, z) ||
+      (f->nt > 1 && !grid_inside(f->gt, f->nt, t))) {
+    o[0] = o[1] = o[2] = NAN;
+    return;
+  }
+  // axes in the interpolator's order; one snapshot drops the time axis
+  const int nd = f->nt > 1 ? 4 : 3;
+  const double* g[4];
+  int n[4];
+  double v[4];
+  int k = 0;
+  if (nd == 4) { g[k] = f->gt; n[k] = f->nt; v[k++] = t; }
+  g[k] = f->gx; n[k] = f->nx; v[k++] = x;
+  g[k] = f->gy; n[k] = f->ny; v[k++] = y;
+  g[k] = f->gz; n[k] = f->nz; v[k++] = z;
+  int idx[4];
+  double w[4];
+  for (int d = 0; d < nd; ++d) idx[d] = grid_cell(g[d], n[d], v[d], &w[d]);
+  double val[3] = {0.0, 0.0, 0.0};
+  for (int corner = 0; corner < (1 << nd); ++corner) {  // bit nd-1-d set: upper corner on axis d
+    double weight = 1.0;
+    int64_t node = 0;
+    for (int d = 0; d < nd; ++d) {
+      const int up = (corner >> (nd - 1 - d)) & 1;
+      weight = weight * (up ? w[d] : 1.0 - w[d]);
+      node = node * n[d] + idx[d] + up;
+    }
+    for (int c = 0; c < 3; ++c) val[c] = val[c] + V[3 * node + c] * weight;
+  }
+  o[0] = val[0]; o[1] = val[1]; o[2] = val[2];
+}
+}  // namespace
 
 // ---------------------------------------------------------------- fields
 void orc_B(const orc_field* f, const double* tpos, double* o) {
@@ -155,6 +215,9 @@ void orc_B(const orc_field* f, const double* tpos, double* o) {
     case ORC_HARRIS:
       o[0] = p[0] * std::tanh(z / p[1]); o[1] = 0; o[2] = p[2];
       return;
+    case ORC_GRID:
+      grid_eval(f, f->gB, tpos, o);
+      return;
     case ORC_COMPRESSED_DIPOLE: {  // VarEarthDipole form with B0(t) = B0 (1 + amp sin(2 pi t / P))
       const double s = -p[0] * (kRe * kRe * kRe) * (1 + p[1] * std::sin(2 * kPi * t / p[2]));
       const double d = std::pow(x * x + y * y + z * z, 5.0 / 2.0);
@@ -172,6 +235,9 @@ void orc_E(const orc_field* f, const double* tpos, double* o) {
   switch (f->model) {
     case ORC_UNIFORM_CROSSED_EB: o[1] = p[0]; return;  // fields.py:413-427
     case ORC_HARRIS: o[1] = p[3]; return;
+    case ORC_GRID:
+      if (f->gE) grid_eval(f, f->gE, tpos, o);
+      return;
     case ORC_COMPRESSED_DIPOLE: {
       // E = -dA/dt with A = B0(t) Re^3 (y, -x, 0) / r^3, whose curl is B above.
       const double t = tpos[0], x = tpos[1], y = tpos[2], z = tpos[3];
@@ -365,6 +431,7 @@ namespace {
 
 struct Counters {
   int64_t nfcn = 0, nstep = 0, naccpt = 0, nrejct = 0;
+  bool stop_nan = false;  // Grid: a NaN error norm means a stage left the grid (idid -6)
 };
 
 // Automatic initial step (Hairer's HINIT, Solving ODEs I, Sec. II.4).
@@ -448,6 +515,7 @@ int dopri5(F& f, int n, double& x, double* y, double xend, double rtol, double a
       err += (k4[i] / sk) * (k4[i] / sk);
     }
     err = std::sqrt(err / n);
+    if (cnt.stop_nan && std::isnan(err)) return -6;
     const double fac11 = std::pow(err, expo1);
     double fac = fac11 / std::pow(facold, beta);
     fac = std::max(facc2, std::min(facc1, fac / safe));
@@ -583,6 +651,7 @@ int dop853(F& f, int n, double& x, double* y, double xend, double rtol, double a
     double deno = err + 0.01 * err2;
     if (deno <= 0.0) deno = 1.0;
     err = std::fabs(h) * err * std::sqrt(1.0 / (n * deno));
+    if (cnt.stop_nan && std::isnan(err)) return -6;
     const double fac11 = std::pow(err, expo1);
     double fac = fac11 / std::pow(facold, beta);
     fac = std::max(facc2, std::min(facc1, fac / safe));
@@ -653,8 +722,13 @@ int rkf45(F& f, int n, double& t, double* x, double b, double tol, double hmax, 
     cnt.nfcn += 6;
     cnt.nstep++;
     double r = 0;
-    for (int i = 0; i < n; ++i)
-      r = std::max(r, std::fabs(r1 * k1[i] + r3 * k3[i] + r4 * k4[i] + r5 * k5[i] + r6 * k6[i]) / h);
+    bool nan_term = false;
+    for (int i = 0; i < n; ++i) {
+      const double ri = std::fabs(r1 * k1[i] + r3 * k3[i] + r4 * k4[i] + r5 * k5[i] + r6 * k6[i]) / h;
+      r = std::max(r, ri);
+      nan_term = nan_term || std::isnan(ri);
+    }
+    if (cnt.stop_nan && nan_term) return -6;
     if (r <= tol) {
       t = t + h;
       for (int i = 0; i < n; ++i) x[i] = x[i] + c1 * k1[i] + c3 * k3[i] + c4 * k4[i] + c5 * k5[i];
@@ -684,6 +758,7 @@ int orc_integrate_particle(const orc_field* f, const orc_config* c, int method, 
                            double beta, int64_t* counters4) {
   auto rhs = [&](double t, const double* Y, double* o) { orc_particle_rhs(f, c, mass, charge, gm, t, Y, o); };
   Counters cnt;
+  cnt.stop_nan = f->model == ORC_GRID;
   int idid;
   if (method == 0) idid = dop853(rhs, 6, *x, y6, xend, c->rtol, c->atol, c->nsteps, cnt, beta);
   else if (method == 1) idid = dopri5(rhs, 6, *x, y6, xend, c->rtol, c->atol, c->nsteps, cnt);
@@ -697,6 +772,7 @@ int orc_integrate_gc(const orc_field* f, const orc_config* c, int method, double
                      int64_t* counters4) {
   auto rhs = [&](double t, const double* Y, double* o) { orc_gc_rhs(f, c, c->gc_eom, mass, charge, mu, v, t, Y, o); };
   Counters cnt;
+  cnt.stop_nan = f->model == ORC_GRID;
   int idid;
   if (method == 0) idid = dop853(rhs, 4, *x, y4, xend, c->rtol, c->atol, c->nsteps, cnt, 0.0);
   else if (method == 1) idid = dopri5(rhs, 4, *x, y4, xend, c->rtol, c->atol, c->nsteps, cnt);
@@ -940,9 +1016,13 @@ int orc_particle_advance(const orc_field* f, const orc_config* c, orc_tracer* p,
     const int method = (c->tableau == 1) ? 2 : 0;
     const int idid = orc_integrate_particle(f, c, method, p->mass, p->charge, gm, &rt, y, rt + dt, 0.1, cnt);
     p->nfcn += cnt[0]; p->nstep += cnt[1]; p->naccept += cnt[2]; p->nreject += cnt[3];
+    if (idid == -6) {  // Grid: the reference raises ValueError inside r.integrate(): no row, state kept
+      p->status = ORC_ST_OUT_OF_GRID;
+      break;
+    }
     if (idid < 0) {
       ok = false;
-      p->status = (idid == -2) ? ORC_ST_MAXSTEPS : (idid == -3) ? ORC_ST_HMIN : ORC_ST_RKF_HMIN;
+      p->status = (idid == -2) ? ORC_ST_MAXSTEPS : (idid == -3) ? ORC_ST_HMIN : (idid == -6) ? ORC_ST_OUT_OF_GRID : ORC_ST_RKF_HMIN;
     }
     if (!finite_n(y, 6)) { p->status = ORC_ST_NONFINITE; ok = false; }
     p->t = rowt;
@@ -972,9 +1052,13 @@ int orc_gc_advance(const orc_field* f, const orc_config* c, orc_tracer* g, doubl
     const int method = (c->tableau == 1) ? 2 : 1;
     const int idid = orc_integrate_gc(f, c, method, g->mass, g->charge, g->mu, g->v, &rt, y, rt + dt, cnt);
     g->nfcn += cnt[0]; g->nstep += cnt[1]; g->naccept += cnt[2]; g->nreject += cnt[3];
+    if (idid == -6) {  // Grid: the reference raises ValueError inside r.integrate(): no row, state kept
+      g->status = ORC_ST_OUT_OF_GRID;
+      break;
+    }
     if (idid < 0) {
       ok = false;
-      g->status = (idid == -2) ? ORC_ST_MAXSTEPS : (idid == -3) ? ORC_ST_HMIN : ORC_ST_RKF_HMIN;
+      g->status = (idid == -2) ? ORC_ST_MAXSTEPS : (idid == -3) ? ORC_ST_HMIN : (idid == -6) ? ORC_ST_OUT_OF_GRID : ORC_ST_RKF_HMIN;
     }
     if (!finite_n(y, 4)) { g->status = ORC_ST_NONFINITE; ok = false; }
     g->t = rt;

@@ -27,7 +27,8 @@ enum {
   ORC_VAR_EARTH_DIPOLE = 4,  /* rapt/fields.py:429-470 */
   ORC_PARABOLIC = 5,         /* rapt/fields.py:472-511 */
   ORC_HARRIS = 6,            /* not in the reference: Harris sheet + uniform Ey */
-  ORC_COMPRESSED_DIPOLE = 7  /* not in the reference: breathing dipole + induced E */
+  ORC_COMPRESSED_DIPOLE = 7, /* not in the reference: breathing dipole + induced E */
+  ORC_GRID = 8               /* rapt/fields.py:513-814 (Grid), data in the grid fields below */
 };
 
 typedef struct {
@@ -36,6 +37,9 @@ typedef struct {
   double p[8];        /* model parameters */
   double gradstep;    /* _Field.gradientstepsize */
   double timestep;    /* _Field.timederivstepsize */
+  /* ORC_GRID: axes and [nt][nx][ny][nz][3] snapshots (host memory, owned by the caller) */
+  const double *gt, *gx, *gy, *gz, *gB, *gE;
+  int nt, nx, ny, nz;
 } orc_field;
 
 typedef struct {
@@ -69,7 +73,7 @@ typedef struct {
 enum {
   ORC_ST_OK = 0, ORC_ST_MAXSTEPS = 2, ORC_ST_HMIN = 3, ORC_ST_NONFINITE = 4,
   ORC_ST_GC_NOCONV = 5, ORC_ST_ROWS_FULL = 6, ORC_ST_BAD_INPUT = 7,
-  ORC_ST_RKF_HMIN = 8, ORC_ST_ADAPTIVE_LIMIT = 9
+  ORC_ST_RKF_HMIN = 8, ORC_ST_ADAPTIVE_LIMIT = 9, ORC_ST_FIELDLINE = 10, ORC_ST_OUT_OF_GRID = 11
 };
 
 void orc_field_init(orc_field* f, int model, const double* params, int nparams);

@@ -14,12 +14,12 @@ LIB_PATH = os.path.join(HERE, "librapt_gpu.so")
 
 RAPT_OK, RAPT_ERR_INVALID, RAPT_ERR_CUDA, RAPT_ERR_NOMEM, RAPT_ERR_UNSUPPORTED, RAPT_ERR_STATE = range(6)
 MODEL_IDS = {"EarthDipole": 0, "DoubleDipole": 1, "UniformBz": 2, "UniformCrossedEB": 3,
-             "VarEarthDipole": 4, "Parabolic": 5, "Harris": 6, "CompressedDipole": 7}
+             "VarEarthDipole": 4, "Parabolic": 5, "Harris": 6, "CompressedDipole": 7, "Grid": 8}
 MODE_PARTICLE, MODE_GC = 0, 1
 KIND_PARTICLE, KIND_GC, KIND_ADAPTIVE = 0, 1, 2
 FORMS = {"plain": 0, "fp32": 1, "learned": 2, "learned_fp32": 3}
 ST = dict(OK=0, MAXSTEPS=2, HMIN=3, NONFINITE=4, GC_NOCONV=5, ROWS_FULL=6, BAD_INPUT=7, FIELDLINE=10,
-          RKF_HMIN=8, ADAPTIVE_LIMIT=9)
+          RKF_HMIN=8, ADAPTIVE_LIMIT=9, OUT_OF_GRID=11)
 FLAG_CHECK, FLAG_RAISED, FLAG_DONE = 1, 2, 4
 FIELD_QUANTITIES = {"B": 0, "E": 1, "gradB": 2, "curlb": 3, "magB": 4, "unitb": 5,
                     "lengthscale": 6, "dbdt": 7, "jacobianB": 8, "dBdt": 9, "timescale": 10}
@@ -64,6 +64,8 @@ SIGNATURES = {
     "rapt_last_error": (C.c_char_p, [_VP]),
     "rapt_field_set": (C.c_int, [_VP, C.c_int, _DP, C.c_int]),
     "rapt_field_set_steps": (C.c_int, [_VP, _D, _D]),
+    "rapt_field_set_static": (C.c_int, [_VP, C.c_int]),
+    "rapt_grid_set": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, _VP, C.c_int32, _VP, C.c_int32, _VP, _VP, _VP]),
     "rapt_config_default": (None, [C.POINTER(RaptConfig)]),
     "rapt_config_set": (C.c_int, [_VP, C.POINTER(RaptConfig)]),
     "rapt_ensemble_alloc": (C.c_int, [_VP, _I64, C.c_int32, C.c_int32]),
@@ -173,6 +175,23 @@ class Context:
         if gradientstepsize is not None or timederivstepsize is not None:
             self.check(self.L.rapt_field_set_steps(self.h, float(gradientstepsize), float(timederivstepsize)),
                        "rapt_field_set_steps")
+
+    def set_static(self, is_static):
+        self.check(self.L.rapt_field_set_static(self.h, 1 if is_static else 0), "rapt_field_set_static")
+
+    def grid_set(self, t, x, y, z, B, E=None):
+        """Upload Grid snapshots (B, E: [nt][nx][ny][nz][3]) and select the Grid model."""
+        a = [np.ascontiguousarray(v, dtype=np.float64) for v in (t, x, y, z)]
+        nt, nx, ny, nz = (len(v) for v in a)
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        if B.shape != (nt, nx, ny, nz, 3):
+            raise ValueError("B must have shape %s, got %s" % ((nt, nx, ny, nz, 3), B.shape))
+        if E is not None:
+            E = np.ascontiguousarray(E, dtype=np.float64)
+            if E.shape != B.shape:
+                raise ValueError("E must have the shape of B")
+        self.check(self.L.rapt_grid_set(self.h, nt, ptr(a[0]), nx, ptr(a[1]), ny, ptr(a[2]), nz, ptr(a[3]),
+                                        ptr(B), ptr(E) if E is not None else None), "rapt_grid_set")
 
     def set_config(self, **kw):
         cfg = RaptConfig()

@@ -48,6 +48,9 @@ struct Ctx {
   unsigned long long* samp_count = nullptr;
   int64_t samp_cap = 0;
   uint64_t samp_mask = 0;
+  // Grid field: axes and snapshots in one device block (rapt_grid_set)
+  double* grid = nullptr;
+  FieldP grid_desc{};  // only the g* pointers and sizes are used
 };
 
 int fail(Ctx* c, int code, const char* fmt, ...) {
@@ -104,10 +107,17 @@ void build_field(int model, const double* params, int np, FieldP* f) {
     case RAPT_PARABOLIC: p[0] = 10.0; p[1] = 1.0; p[2] = 0.2; break;
     case RAPT_HARRIS: p[0] = 20e-9; p[1] = 0.5 * kRe; p[2] = 2e-9; p[3] = 0.2e-3; f->is_static = 0; break;
     case RAPT_COMPRESSED_DIPOLE: p[0] = kB0; p[1] = 0.1; p[2] = 60.0; f->gradstep = kRe / 1000; f->is_static = 0; break;
+    case RAPT_GRID: f->gradstep = 1e-3 * kRe; break;  // fields.py:578; static stays 1 (fields.py:41)
     default: break;
   }
   for (int i = 0; i < np && i < 8; ++i) p[i] = params[i];
   if (model == RAPT_HARRIS) f->gradstep = p[1] * 1e-4;
+}
+
+void attach_grid(const FieldP& g, FieldP* f) {
+  f->gt = g.gt; f->gx = g.gx; f->gy = g.gy; f->gz = g.gz;
+  f->gB = g.gB; f->gE = g.gE;
+  f->nt = g.nt; f->nx = g.nx; f->ny = g.ny; f->nz = g.nz;
 }
 
 void finish_field(FieldP* f) {
@@ -247,6 +257,7 @@ int rapt_ctx_create(int device, void** out) {
   register_model_5(&c->tab[5]);
   register_model_6(&c->tab[6]);
   register_model_7(&c->tab[7]);
+  register_model_8(&c->tab[8]);
   rapt_config_default(&c->cfg);
   *out = c;
   return RAPT_OK;
@@ -263,6 +274,7 @@ void rapt_ctx_destroy(void* ctx) {
   cudaFree(c->mlp_block);
   cudaFree(c->fl_scratch);
   cudaFree(c->samp_count);  // base of the sample allocation
+  cudaFree(c->grid);
   cudaFreeHost(c->h_pending);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -281,7 +293,9 @@ int rapt_field_set(void* ctx, int model, const double* params, int nparams) {
   if (model < 0 || model >= RAPT_N_MODELS)
     return fail(c, RAPT_ERR_UNSUPPORTED, "field model %d has no device implementation", model);
   if (nparams < 0 || nparams > 8 || (nparams > 0 && !params)) return fail(c, RAPT_ERR_INVALID, "bad field params");
+  if (model == RAPT_GRID && !c->grid) return fail(c, RAPT_ERR_STATE, "no grid data: call rapt_grid_set");
   build_field(model, params, nparams, &c->field);
+  if (model == RAPT_GRID) attach_grid(c->grid_desc, &c->field);
   if (model == RAPT_DOUBLE_DIPOLE && !(c->field.p[2] >= 1))
     return fail(c, RAPT_ERR_INVALID, "DoubleDipole imagestrength must be >= 1 (fields.py:340)");
   finish_field(&c->field);
@@ -297,6 +311,64 @@ int rapt_field_set_steps(void* ctx, double gradientstepsize, double timederivste
   c->field.gradstep = gradientstepsize;
   c->field.timestep = timederivstepsize;
   finish_field(&c->field);
+  return RAPT_OK;
+}
+
+int rapt_field_set_static(void* ctx, int is_static) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c) return RAPT_ERR_INVALID;
+  if (!c->field_set) return fail(c, RAPT_ERR_STATE, "no field set");
+  c->field.is_static = is_static ? 1 : 0;
+  return RAPT_OK;
+}
+
+static bool ascending(const double* a, int n) {
+  for (int i = 0; i < n; ++i)
+    if (!std::isfinite(a[i]) || (i > 0 && !(a[i] > a[i - 1]))) return false;
+  return true;
+}
+
+int rapt_grid_set(void* ctx, int32_t nt, const double* t, int32_t nx, const double* x, int32_t ny, const double* y,
+                  int32_t nz, const double* z, const double* B, const double* E) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c) return RAPT_ERR_INVALID;
+  if (nt < 1 || nx < 2 || ny < 2 || nz < 2 || !t || !x || !y || !z || !B)
+    return fail(c, RAPT_ERR_INVALID, "grid: need nt >= 1 snapshots, >= 2 points per axis, axes and B");
+  if (!ascending(t, nt) || !ascending(x, nx) || !ascending(y, ny) || !ascending(z, nz))
+    return fail(c, RAPT_ERR_INVALID, "grid: times and axes must be finite and strictly ascending");
+  const size_t nodes = (size_t)nt * (size_t)nx * (size_t)ny * (size_t)nz;
+  if (nodes > ((size_t)1 << 36)) return fail(c, RAPT_ERR_INVALID, "grid: too many nodes");
+  const size_t naxis = (size_t)nt + nx + ny + nz;
+  const size_t words = naxis + 3 * nodes * (E ? 2 : 1);
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->grid) {
+    CK(cudaFree(c->grid));
+    c->grid = nullptr;
+    if (c->field_set && c->field.model == RAPT_GRID) c->field_set = false;
+  }
+  double* d = nullptr;
+  if (cudaMalloc(&d, words * sizeof(double)) != cudaSuccess)
+    return fail(c, RAPT_ERR_NOMEM, "grid: cannot allocate %zu bytes", words * sizeof(double));
+  c->grid = d;
+  // [B | E | t | x | y | z]: the snapshot arrays first keep them 256-byte aligned
+  double* dB = d;
+  double* dE = E ? d + 3 * nodes : nullptr;
+  double* da = d + 3 * nodes * (E ? 2 : 1);
+  CK(cudaMemcpy(dB, B, 3 * nodes * sizeof(double), cudaMemcpyHostToDevice));
+  if (E) CK(cudaMemcpy(dE, E, 3 * nodes * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(da, t, nt * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(da + nt, x, nx * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(da + nt + nx, y, ny * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(da + nt + nx + ny, z, nz * sizeof(double), cudaMemcpyHostToDevice));
+  FieldP& g = c->grid_desc;
+  g.gB = dB; g.gE = dE;
+  g.gt = da; g.gx = da + nt; g.gy = da + nt + nx; g.gz = da + nt + nx + ny;
+  g.nt = nt; g.nx = nx; g.ny = ny; g.nz = nz;
+  build_field(RAPT_GRID, nullptr, 0, &c->field);
+  attach_grid(g, &c->field);
+  finish_field(&c->field);
+  c->field_set = true;
   return RAPT_OK;
 }
 

@@ -27,6 +27,10 @@ struct FieldP {
   double inv2d;       // 1 / (2 gradstep)
   double c0, c1, c2;  // model constants precomputed on the host
   float dh[4], dl[4]; // float-float model constants (hi, lo) for the FP32 form
+  // RAPT_GRID: axes and [nt][nx][ny][nz][3] snapshots resident on the device
+  const double *gt, *gx, *gy, *gz;
+  const double *gB, *gE;  // gE null: zero electric field
+  int nt, nx, ny, nz;
 };
 
 // rapt.params plus device options, resolved on the host.

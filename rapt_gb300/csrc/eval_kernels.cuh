@@ -37,7 +37,7 @@ __global__ void k_field_eval(FieldP f, int what, int64_t n, const double* tpos, 
       break;
     case 9: r[0] = dBdt<M>(f, t, X); break;
     case 10: {
-      if (Field<M>::kStatic) { r[0] = nan(""); break; }
+      if (field_static<M>(f)) { r[0] = nan(""); break; }
       double u[3], m;
       unit_and_mag<M>(f, t, X[0], X[1], X[2], u, m);
       r[0] = m / fabs(dBdt<M>(f, t, X));

@@ -163,6 +163,110 @@ struct Field<RAPT_COMPRESSED_DIPOLE> {
   }
 };
 
+// Grid, fields.py:513-814 (Bgrid :707-738, Egrid :740-771): SciPy's
+// RegularGridInterpolator, method "linear", over (t, x, y, z), or (x, y, z)
+// for a single snapshot, restated from SciPy's _rgi.py _evaluate_linear and
+// find_indices. Per axis the cell i with g[i] <= v < g[i+1] (the last cell for
+// v == g[n-1]) and w = (v - g[i]) / (g[i+1] - g[i]); the 2^d corners in
+// itertools.product order (last axis fastest), the lower corner weighted 1 - w
+// and the upper w; a corner's weight is the running product over the axes, and
+// the value is summed corner by corner from 0. Every product and sum is rounded
+// on its own (no FMA), as numpy evaluates them, so values agree bit for bit.
+// Outside the grid (or at a NaN coordinate) the reference raises ValueError
+// from the interpolator's bounds check; here each component is NaN, which the
+// steppers report as RAPT_ST_OUT_OF_GRID.
+struct GridV {
+  double a, b, c;
+};
+
+// Cell index and normalised distance on a strictly ascending axis; v in [g[0], g[n-1]].
+__device__ __forceinline__ int grid_cell(const double* __restrict__ g, int n, double v, double& w) {
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(g + mid) <= v) lo = mid;
+    else hi = mid;
+  }
+  const double g0 = __ldg(g + lo);
+  w = (v - g0) / (__ldg(g + lo + 1) - g0);
+  return lo;
+}
+
+__device__ __forceinline__ bool grid_inside(const double* __restrict__ g, int n, double v) {
+  return __ldg(g) <= v && v <= __ldg(g + n - 1);
+}
+
+// One interpolation of a [nt][nx][ny][nz][3] array: not inlined, so that the
+// seven B evaluations of a guiding-centre right-hand side share one copy.
+static __device__ __noinline__ GridV grid_interp(const double* __restrict__ gt, const double* __restrict__ gx,
+                                                 const double* __restrict__ gy, const double* __restrict__ gz,
+                                                 const double* __restrict__ V, int nt, int nx, int ny, int nz,
+                                                 double t, double x, double y, double z) {
+  const double qnan = __longlong_as_double(0x7ff8000000000000LL);
+  if (!grid_inside(gx, nx, x) || !grid_inside(gy, ny, y) || !grid_inside(gz, nz, z) ||
+      (nt > 1 && !grid_inside(gt, nt, t)))
+    return GridV{qnan, qnan, qnan};
+  double wx, wy, wz, wt = 1.0;
+  const int ix = grid_cell(gx, nx, x, wx);
+  const int iy = grid_cell(gy, ny, y, wy);
+  const int iz = grid_cell(gz, nz, z, wz);
+  int it = 0;
+  if (nt > 1) it = grid_cell(gt, nt, t, wt);
+  const int64_t sy = nz, sx = (int64_t)ny * nz, st = (int64_t)nx * sx;
+  // one snapshot: weights (1 * wx) * wy * wz, the same products as the 3-D
+  // interpolator's, since 1 * w == w
+  const int ntc = nt > 1 ? 2 : 1;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int ct = 0; ct < ntc; ++ct) {
+    const double w1 = ntc == 1 ? 1.0 : (ct ? wt : 1.0 - wt);
+#pragma unroll
+    for (int cx = 0; cx < 2; ++cx) {
+      const double w2 = __dmul_rn(w1, cx ? wx : 1.0 - wx);
+#pragma unroll
+      for (int cy = 0; cy < 2; ++cy) {
+        const double w3 = __dmul_rn(w2, cy ? wy : 1.0 - wy);
+        const double* p = V + 3 * ((it + ct) * st + (ix + cx) * sx + (iy + cy) * sy + iz);
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz) {
+          const double w = __dmul_rn(w3, cz ? wz : 1.0 - wz);
+          s0 = __dadd_rn(s0, __dmul_rn(__ldg(p + 3 * cz + 0), w));
+          s1 = __dadd_rn(s1, __dmul_rn(__ldg(p + 3 * cz + 1), w));
+          s2 = __dadd_rn(s2, __dmul_rn(__ldg(p + 3 * cz + 2), w));
+        }
+      }
+    }
+  }
+  return GridV{s0, s1, s2};
+}
+
+template <>
+struct Field<RAPT_GRID> {
+  static constexpr bool kStatic = false;  // the runtime flag f.is_static decides (field_static)
+  __device__ __forceinline__ static void B(const FieldP& f, double t, double x, double y, double z, double* o) {
+    const GridV r = grid_interp(f.gt, f.gx, f.gy, f.gz, f.gB, f.nt, f.nx, f.ny, f.nz, t, x, y, z);
+    o[0] = r.a; o[1] = r.b; o[2] = r.c;
+  }
+  __device__ __forceinline__ static void E(const FieldP& f, double t, double x, double y, double z, double* o) {
+    if (!f.gE) { o[0] = o[1] = o[2] = 0.0; return; }
+    const GridV r = grid_interp(f.gt, f.gx, f.gy, f.gz, f.gE, f.nt, f.nx, f.ny, f.nz, t, x, y, z);
+    o[0] = r.a; o[1] = r.b; o[2] = r.c;
+  }
+};
+
+// _Field.static (fields.py:41): fixed by the equations of the analytic models,
+// the runtime attribute for Grid (which leaves it True by default).
+template <int M>
+__device__ __forceinline__ bool field_static(const FieldP& f) {
+  return Field<M>::kStatic || (M == RAPT_GRID && f.is_static);
+}
+
+// A step whose error norm is NaN evaluated a Grid field outside the grid: the
+// reference raises ValueError there, the steppers stop with RAPT_ST_OUT_OF_GRID.
+template <int M>
+__device__ __forceinline__ bool left_grid(double err) {
+  return M == RAPT_GRID && isnan(err);
+}
+
 // Unit vector and magnitude of B at a point: one rsqrt.
 template <int M>
 __device__ __forceinline__ void unit_and_mag(const FieldP& f, double t, double x, double y, double z, double* ub,
@@ -202,7 +306,7 @@ __device__ __forceinline__ void stencil_gradB_curlb(const FieldP& f, double t, c
 // db/dt by central differences in time (fields.py:225-245); zero when static.
 template <int M>
 __device__ __forceinline__ void dbdt(const FieldP& f, double t, const double* X, double* o) {
-  if (Field<M>::kStatic) { o[0] = o[1] = o[2] = 0.0; return; }
+  if (field_static<M>(f)) { o[0] = o[1] = o[2] = 0.0; return; }
   double u1[3], u2[3], m1, m2;
   unit_and_mag<M>(f, t - f.timestep, X[0], X[1], X[2], u1, m1);
   unit_and_mag<M>(f, t + f.timestep, X[0], X[1], X[2], u2, m2);
@@ -213,7 +317,7 @@ __device__ __forceinline__ void dbdt(const FieldP& f, double t, const double* X,
 // d|B|/dt (fields.py:202-223).
 template <int M>
 __device__ __forceinline__ double dBdt(const FieldP& f, double t, const double* X) {
-  if (Field<M>::kStatic) return 0.0;
+  if (field_static<M>(f)) return 0.0;
   double u[3], m1, m2;
   unit_and_mag<M>(f, t - f.timestep, X[0], X[1], X[2], u, m1);
   unit_and_mag<M>(f, t + f.timestep, X[0], X[1], X[2], u, m2);

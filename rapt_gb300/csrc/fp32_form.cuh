@@ -142,7 +142,7 @@ struct ParticleRHSdf {
   bool eq;
   __device__ __forceinline__ void operator()(double t, const DF* Y, DF* o) const {
     DF ig = igam;
-    if (!Field<M>::kStatic) ig = df_rsqrt(DF{1.f, 0.f} + Y[3] * Y[3] + Y[4] * Y[4] + Y[5] * Y[5]);
+    if (!field_static<M>(f)) ig = df_rsqrt(DF{1.f, 0.f} + Y[3] * Y[3] + Y[4] * Y[4] + Y[5] * Y[5]);
     DF B[3], E[3];
     FieldDF<M>::B(f, t, Y, B);
     FieldDF<M>::E(f, t, Y, E);

@@ -91,7 +91,8 @@ __global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P,
     if (!in_interval) {
       if (!(seg_ok && rt < stop)) {
         bool more = false;
-        if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && tcur < delta) {
+        if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_OUT_OF_GRID &&
+            tcur < delta) {
           if (nseg + 1 >= P.max_segments) {
             status = RAPT_ST_ADAPTIVE_LIMIT;
           } else {
@@ -148,7 +149,10 @@ __global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P,
       double fac = fac11 / facold_beta;
       fac = fmax(facc2, fmin(facc1, fac / safe));
       double hnew = h / fac;
-      if (err <= 1.0) {
+      if (left_grid<M>(err)) {
+        ended = true;
+        fail = RAPT_ST_OUT_OF_GRID;
+      } else if (err <= 1.0) {
         facold_beta = powf_fast(fmax(err, 1.0e-4), (float)beta);
         ++nacc; ++nacc_int; st.acc++;
         const double xph = rt + h;
@@ -181,10 +185,14 @@ __global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P,
       state_si(s);
       if (fail) { seg_ok = false; status = fail; }
       if (!all_finite<6>(s)) { seg_ok = false; status = RAPT_ST_NONFINITE; }
-      t_row = rowt;
-      tcur = rt + dt;
-      put_row(E, P, idx, nrows, rowt, s, 6, RAPT_MODE_PARTICLE);
-      if ((flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE &&
+      // a Grid step outside the grid: the reference raises inside the interval, adding no row
+      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID);
+      if (row) {
+        t_row = rowt;
+        tcur = rt + dt;
+        put_row(E, P, idx, nrows, rowt, s, 6, RAPT_MODE_PARTICLE);
+      }
+      if (row && (flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE &&
           particle_isadiabatic<M>(P, t_row, s, mass, charge)) {
         if (P.kind == RAPT_KIND_ADAPTIVE) {
           double g[6], mu, vs;
@@ -335,7 +343,7 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
       if (!(seg_ok && rt < stop)) {
         bool more = false;
         if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_BAD_INPUT &&
-            tcur < delta) {
+            status != RAPT_ST_OUT_OF_GRID && tcur < delta) {
           if (nseg + 1 >= P.max_segments) {
             status = RAPT_ST_ADAPTIVE_LIMIT;
           } else {
@@ -400,7 +408,10 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
       double fac = fac11 / facold_beta;
       fac = fmax(facc2, fmin(facc1, fac / safe));
       double hnew = h / fac;
-      if (err <= 1.0) {
+      if (left_grid<M>(err)) {
+        ended = true;
+        fail = RAPT_ST_OUT_OF_GRID;
+      } else if (err <= 1.0) {
         const double errprev = errold;
         const bool rej_before = reject;
         const double hstep = h;
@@ -438,10 +449,14 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
       state_si(s);
       if (fail) { seg_ok = false; status = fail; }
       if (!all_finite<4>(s)) { seg_ok = false; status = RAPT_ST_NONFINITE; }
-      t_row = rt;
-      tcur = rt;
-      put_row(E, P, idx, nrows, rt, s, 4, RAPT_MODE_GC);
-      const bool row_chk = (flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE;
+      // a Grid step outside the grid: the reference raises inside the interval, adding no row
+      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID);
+      if (row) {
+        t_row = rt;
+        tcur = rt;
+        put_row(E, P, idx, nrows, rt, s, 4, RAPT_MODE_GC);
+      }
+      const bool row_chk = row && (flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE;
       const bool nonadi = row_chk && !gc_isadiabatic<M>(P, t_row, s, mu, mass, charge);
       if (row_chk) lr.on_row(P, nonadi);
       if (nonadi) {

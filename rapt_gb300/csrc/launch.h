@@ -59,5 +59,6 @@ void register_model_4(ModelTable*);
 void register_model_5(ModelTable*);
 void register_model_6(ModelTable*);
 void register_model_7(ModelTable*);
+void register_model_8(ModelTable*);
 
 }  // namespace rapt

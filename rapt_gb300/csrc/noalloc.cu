@@ -139,6 +139,7 @@ extern "C" int rapt_gc_advance_noalloc(int device, int model, const double* para
   if (!cfg || !st) return RAPT_ERR_INVALID;
   if (st->n < 0 || st->n > kMax) return RAPT_ERR_INVALID;  // more tracers than the scratch holds
   if (model < 0 || model >= RAPT_N_MODELS) return RAPT_ERR_UNSUPPORTED;
+  if (model == RAPT_GRID) return RAPT_ERR_UNSUPPORTED;  // its data live in a context (rapt_grid_set)
   if (nparams < 0 || nparams > 8 || (nparams > 0 && !params)) return RAPT_ERR_INVALID;
   if (!std::isfinite(delta) || cfg->tableau < 0 || cfg->tableau > 1 || cfg->gc_eom < 0 || cfg->gc_eom > 2 ||
       cfg->nsteps <= 0 || st->max_rows < 2)

@@ -15,7 +15,7 @@ struct ParticleRHS {
   bool eq;
   __device__ __forceinline__ void operator()(double t, const double* Y, double* o) const {
     double igm = inv_gm_frozen;
-    if (!Field<M>::kStatic) igm = rsqrt(mass2 + (Y[3] * Y[3] + Y[4] * Y[4] + Y[5] * Y[5]) * (1.0 / (kC * kC)));
+    if (!field_static<M>(f)) igm = rsqrt(mass2 + (Y[3] * Y[3] + Y[4] * Y[4] + Y[5] * Y[5]) * (1.0 / (kC * kC)));
     double B[3], E[3];
     Field<M>::B(f, t, Y[0], Y[1], Y[2], B);
     Field<M>::E(f, t, Y[0], Y[1], Y[2], E);

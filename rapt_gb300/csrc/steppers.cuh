@@ -260,8 +260,9 @@ __device__ __forceinline__ void dop853_attempt(const F& f, double x, const doubl
 }
 
 // One RKF45 attempt as restated from rapt/rkf.py:101-124: k_i = h f(...),
-// error r = max_i |sum r_j k_j| / h, 4th-order solution y1.
-template <int NV, class F>
+// error r = max_i |sum r_j k_j| / h, 4th-order solution y1. NANPROP: r is NaN
+// when any term is (a Grid stage outside the grid), which fmax alone would drop.
+template <int NV, bool NANPROP = false, class F>
 __device__ __forceinline__ void rkf45_attempt(const F& f, double t, const double* x, double h, double* y1,
                                               double& r) {
   constexpr double a2 = 0.25, a3 = 0.375, a4 = 12.0 / 13.0, a5 = 1.0, a6 = 0.5;
@@ -293,12 +294,16 @@ __device__ __forceinline__ void rkf45_attempt(const F& f, double t, const double
   }
   f(t + a6 * h, xt, k6);
   r = 0.0;
+  bool nan_term = false;
 #pragma unroll
   for (int i = 0; i < NV; ++i) {
     k6[i] *= h;
-    r = fmax(r, fabs(r1 * k1[i] + r3 * k3[i] + r4 * k4[i] + r5 * k5[i] + r6 * k6[i]) / h);
+    const double ri = fabs(r1 * k1[i] + r3 * k3[i] + r4 * k4[i] + r5 * k5[i] + r6 * k6[i]) / h;
+    r = fmax(r, ri);
+    if (NANPROP) nan_term = nan_term || isnan(ri);
     y1[i] = x[i] + c1 * k1[i] + c3 * k3[i] + c4 * k4[i] + c5 * k5[i];
   }
+  if (NANPROP && nan_term) r = __longlong_as_double(0x7ff8000000000000LL);
 }
 
 }  // namespace rapt

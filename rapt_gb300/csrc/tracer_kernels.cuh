@@ -63,7 +63,7 @@ __device__ bool particle_isadiabatic(const KParams& P, double t, const double* s
   const double vperp = sqrt(vsq - vpar * vpar);
   const double cycrad = gamma * mass * vperp / (fabs(charge) * Bmag);
   const bool sp = cycrad / lengthscale<M>(f, t, s) < P.epss;
-  if (Field<M>::kStatic) return sp;
+  if (field_static<M>(f)) return sp;
   if (!sp) return false;
   const double cycper = cyc_period_vel<M>(f, t, s, v, mass, charge);
   const double ts = Bmag / fabs(dBdt<M>(f, t, s));
@@ -87,7 +87,7 @@ __device__ bool gc_isadiabatic(const KParams& P, double t, const double* s, doub
   const double g2 = 1.0 / sqrt(1.0 - (v / kC) * (v / kC));
   const double cycrad = g2 * m * sqrt((v - vp) * (v + vp)) / (fabs(charge) * Bmag);
   const bool sp = cycrad / lengthscale<M>(f, t, s) < P.epss;
-  if (Field<M>::kStatic) return sp;
+  if (field_static<M>(f)) return sp;
   if (!sp) return false;
   const double gq = sqrt(1.0 + 2.0 * mu * Bmag / (m * kC * kC) + pp * pp);
   double v2;
@@ -337,7 +337,8 @@ __global__ void __launch_bounds__(128) k_particle(DevEnsemble E, KParams P, Scra
       if (!(seg_ok && rt < stop)) {
         // end of this Particle.advance() call
         bool more = false;
-        if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && tcur < delta) {
+        if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_OUT_OF_GRID &&
+            tcur < delta) {
           if (nseg + 1 >= P.max_segments) {
             status = RAPT_ST_ADAPTIVE_LIMIT;
           } else {
@@ -406,7 +407,10 @@ __global__ void __launch_bounds__(128) k_particle(DevEnsemble E, KParams P, Scra
         double fac = fac11 / pow(facold, beta);
         fac = fmax(facc2, fmin(facc1, fac / safe));
         double hnew = h / fac;
-        if (err <= 1.0) {
+        if (left_grid<M>(err)) {
+          ended = true;
+          fail = RAPT_ST_OUT_OF_GRID;
+        } else if (err <= 1.0) {
           facold = fmax(err, 1.0e-4);
           ++nacc; ++nacc_int; st.acc++;
           const double xph = rt + h;
@@ -440,23 +444,28 @@ __global__ void __launch_bounds__(128) k_particle(DevEnsemble E, KParams P, Scra
       else {
         if (rt + h > xend) h = xend - rt;
         double y1[6], r;
-        rkf45_attempt<6>(rhs, rt, y, h, y1, r);
+        rkf45_attempt<6, M == RAPT_GRID>(rhs, rt, y, h, y1, r);
         ++nst;
         --budget;
         nfcn += 6;
         st.rhs += 6;
-        if (r <= P.rkf_tol) {
-          rt = rt + h;
-#pragma unroll
-          for (int i = 0; i < 6; ++i) y[i] = y1[i];
-          ++nacc; st.acc++;
+        if (left_grid<M>(r)) {
+          ended = true;
+          fail = RAPT_ST_OUT_OF_GRID;
         } else {
-          ++nrej; st.rej++;
+          if (r <= P.rkf_tol) {
+            rt = rt + h;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) y[i] = y1[i];
+            ++nacc; st.acc++;
+          } else {
+            ++nrej; st.rej++;
+          }
+          h = h * fmin(fmax(0.84 * pow(P.rkf_tol / r, 0.25), 0.1), 4.0);
+          if (h > hmax) h = hmax;
+          else if (h < P.rkf_hmin) { ended = true; fail = RAPT_ST_RKF_HMIN; }
+          if (!ended && !(rt < xend)) ended = true;
         }
-        h = h * fmin(fmax(0.84 * pow(P.rkf_tol / r, 0.25), 0.1), 4.0);
-        if (h > hmax) h = hmax;
-        else if (h < P.rkf_hmin) { ended = true; fail = RAPT_ST_RKF_HMIN; }
-        if (!ended && !(rt < xend)) ended = true;
       }
     }
 
@@ -464,10 +473,14 @@ __global__ void __launch_bounds__(128) k_particle(DevEnsemble E, KParams P, Scra
       in_interval = false;
       if (fail) { seg_ok = false; status = fail; }
       if (!all_finite<6>(y)) { seg_ok = false; status = RAPT_ST_NONFINITE; }
-      t_row = rowt;
-      tcur = rt + dt;  // Particle.py:306
-      put_row(E, P, idx, nrows, rowt, y, 6, RAPT_MODE_PARTICLE);
-      if ((flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE &&
+      // a Grid step outside the grid: the reference raises inside the interval, adding no row
+      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID);
+      if (row) {
+        t_row = rowt;
+        tcur = rt + dt;  // Particle.py:306
+        put_row(E, P, idx, nrows, rowt, y, 6, RAPT_MODE_PARTICLE);
+      }
+      if (row && (flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE &&
           particle_isadiabatic<M>(P, t_row, y, mass, charge)) {
         if (P.kind == RAPT_KIND_ADAPTIVE) {
           double g[6], mu, vs;
@@ -609,7 +622,7 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
       if (!(seg_ok && rt < stop)) {
         bool more = false;
         if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_BAD_INPUT &&
-            tcur < delta) {
+            status != RAPT_ST_OUT_OF_GRID && tcur < delta) {
           if (nseg + 1 >= P.max_segments) {
             status = RAPT_ST_ADAPTIVE_LIMIT;
           } else {
@@ -684,7 +697,10 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
         double fac = fac11 / pow(facold, beta);
         fac = fmax(facc2, fmin(facc1, fac / safe));
         double hnew = h / fac;
-        if (err <= 1.0) {
+        if (left_grid<M>(err)) {
+          ended = true;
+          fail = RAPT_ST_OUT_OF_GRID;
+        } else if (err <= 1.0) {
           const double errprev = facold;
           const bool rej_before = reject;
           const double hstep = h;
@@ -721,23 +737,28 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
       else {
         if (rt + h > xend) h = xend - rt;
         double y1[4], r;
-        rkf45_attempt<4>(rhs, rt, y, h, y1, r);
+        rkf45_attempt<4, M == RAPT_GRID>(rhs, rt, y, h, y1, r);
         ++nst;
         --budget;
         nfcn += 6;
         st.rhs += 6;
-        if (r <= P.rkf_tol) {
-          rt = rt + h;
-#pragma unroll
-          for (int i = 0; i < 4; ++i) y[i] = y1[i];
-          ++nacc; st.acc++;
+        if (left_grid<M>(r)) {
+          ended = true;
+          fail = RAPT_ST_OUT_OF_GRID;
         } else {
-          ++nrej; st.rej++;
+          if (r <= P.rkf_tol) {
+            rt = rt + h;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) y[i] = y1[i];
+            ++nacc; st.acc++;
+          } else {
+            ++nrej; st.rej++;
+          }
+          h = h * fmin(fmax(0.84 * pow(P.rkf_tol / r, 0.25), 0.1), 4.0);
+          if (h > hmax) h = hmax;
+          else if (h < P.rkf_hmin) { ended = true; fail = RAPT_ST_RKF_HMIN; }
+          if (!ended && !(rt < xend)) ended = true;
         }
-        h = h * fmin(fmax(0.84 * pow(P.rkf_tol / r, 0.25), 0.1), 4.0);
-        if (h > hmax) h = hmax;
-        else if (h < P.rkf_hmin) { ended = true; fail = RAPT_ST_RKF_HMIN; }
-        if (!ended && !(rt < xend)) ended = true;
       }
     }
 
@@ -745,10 +766,14 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
       in_interval = false;
       if (fail) { seg_ok = false; status = fail; }
       if (!all_finite<4>(y)) { seg_ok = false; status = RAPT_ST_NONFINITE; }
-      t_row = rt;
-      tcur = rt;
-      put_row(E, P, idx, nrows, rt, y, 4, RAPT_MODE_GC);
-      const bool row_chk = (flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE;
+      // a Grid step outside the grid: the reference raises inside the interval, adding no row
+      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID);
+      if (row) {
+        t_row = rt;
+        tcur = rt;
+        put_row(E, P, idx, nrows, rt, y, 4, RAPT_MODE_GC);
+      }
+      const bool row_chk = row && (flags & RAPT_FLAG_CHECK_ADIABATICITY) && status != RAPT_ST_NONFINITE;
       const bool nonadi = row_chk && !gc_isadiabatic<M>(P, t_row, y, mu, mass, charge);
       if (row_chk) lr.on_row(P, nonadi);
       if (nonadi) {

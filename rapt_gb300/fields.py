@@ -5,9 +5,9 @@ Each class keeps the reference constructor, its ``gradientstepsize``,
 The methods are evaluated by the GPU library (``rapt_field_eval``) and accept
 either one (t, x, y, z) point, as in the reference, or an (n, 4) array.
 
-A field with no device implementation -- ``Grid``, or any subclass that
-overrides ``B`` or ``E`` -- raises ``NotImplementedError`` when a tracer is
-advanced with it; there is no CPU fallback.
+A field with no device implementation -- any subclass that overrides ``B``
+or ``E`` -- raises ``NotImplementedError`` when a tracer is advanced with it;
+there is no CPU fallback.
 """
 import numpy as np
 
@@ -221,13 +221,100 @@ class CompressedDipole(_Field):
 
 
 class Grid(_Field):
-    """Gridded fields (rapt/fields.py:513-814) have no device implementation."""
-    model_id = None
+    """Gridded fields, rapt/fields.py:513-814, interpolated on the device.
 
-    def __init__(self, *args, **kwargs):
+    Subclass and override ``parsefile`` as in the reference: it returns a dict
+    with "time", the axes "x", "y", "z" and the 3-D arrays "Bx" .. "Ez" of one
+    snapshot. The constructor parses every file of ``filelist`` (ordered in time)
+    and uploads all snapshots to the device on first use; the reference keeps a
+    window of three and re-parses as tracers move (fields.py:695-705), which gives
+    the same interpolated values. One file: a time-independent field (3-D
+    interpolation). Interpolation is SciPy's RegularGridInterpolator "linear",
+    restated bit for bit in the device kernels.
+
+    ``B``/``E`` (or ``Bgrid``/``Egrid``) outside the grid raise ValueError as the
+    reference's interpolator does; a tracer that steps outside the grid stops
+    with status OUT_OF_GRID. ``static`` stays True as in the reference
+    (fields.py:41): set it to False for time-dependent data or a nonzero E.
+    """
+    model_id = N.MODEL_IDS["Grid"]
+    _uids = iter(range(1, 1 << 62))
+
+    def __init__(self, filelist):
+        assert len(filelist) > 0
         _Field.__init__(self)
+        self.gradientstepsize = 1e-3 * Re  # fields.py:578
+        snaps = [self.parsefile(fn) for fn in filelist]
+        g0 = snaps[0]
+        self._x, self._y, self._z = (np.ascontiguousarray(g0[k], dtype=np.float64) for k in ("x", "y", "z"))
+        for g in snaps[1:]:
+            for k in ("x", "y", "z"):
+                if not np.array_equal(np.asarray(g[k], dtype=np.float64), getattr(self, "_" + k)):
+                    raise ValueError("grid coordinates must be the same in every file")
+        self._t = np.array([float(g["time"]) for g in snaps])
+        self._B = np.ascontiguousarray(np.stack([np.stack([g["Bx"], g["By"], g["Bz"]], -1) for g in snaps]),
+                                       dtype=np.float64)
+        E = np.ascontiguousarray(np.stack([np.stack([g["Ex"], g["Ey"], g["Ez"]], -1) for g in snaps]),
+                                 dtype=np.float64)
+        self._E = None if not np.any(E) else E  # all-zero E: the kernels skip the loads
+        self._finite = bool(np.isfinite(self._B).all() and (self._E is None or np.isfinite(self._E).all()))
+        self._time_indep = len(snaps) == 1
+        self.t0 = self._t[0]
+        if len(snaps) >= 2:
+            self.t1 = self._t[1]
+        if len(snaps) >= 3:
+            self.t2 = self._t[2]
+        self.files = []  # every file has been parsed
+        self._uid = next(Grid._uids)
+
+    def parsefile(self, filename):
+        """Parse one snapshot file (fields.py:599-625); override when subclassing."""
+        return dict()
+
+    def bind(self, ctx):
+        if not self.has_device_impl():
+            raise NotImplementedError("%s overrides B or E; rapt_gb300 has no CPU fallback" % type(self).__name__)
+        if getattr(ctx, "_grid_uid", None) != self._uid:
+            ctx.grid_set(self._t, self._x, self._y, self._z, self._B, self._E)
+            ctx._grid_uid = self._uid
+        ctx.set_field(self.model_id, (), self.gradientstepsize, self.timederivstepsize)
+        ctx.set_static(self.static)
+
+    def _check_bounds(self, tpos):
+        # RegularGridInterpolator's bounds check (bounds_error=True)
+        tp = np.atleast_2d(np.asarray(tpos, dtype=np.float64))
+        axes = [self._x, self._y, self._z]
+        cols = [1, 2, 3]
+        if not self._time_indep:
+            axes, cols = [self._t] + axes, [0] + cols
+        for d, (g, c) in enumerate(zip(axes, cols)):
+            p = tp[:, c]
+            if not np.logical_and(np.all(g[0] <= p), np.all(p <= g[-1])):
+                raise ValueError("One of the requested xi is out of bounds in dimension %d" % d)
+
+    def _eval(self, what, tpos):
+        if what in ("B", "E"):
+            self._check_bounds(tpos)
+        out = _Field._eval(self, what, tpos)
+        if self._finite and np.isnan(out).any():
+            raise ValueError("One of the requested xi is out of bounds (a difference stencil left the grid)")
+        return out
+
+    def Bgrid(self, tpos):
+        """fields.py:707-738."""
+        return _Field.B(self, tpos)
+
+    def Egrid(self, tpos):
+        """fields.py:740-771."""
+        return _Field.E(self, tpos)
+
+    def B(self, tpos):
+        return self.Bgrid(tpos)
+
+    def E(self, tpos):
+        return self.Egrid(tpos)
 
 
 for _cls in (EarthDipole, DoubleDipole, UniformBz, UniformCrossedEB, VarEarthDipole, Parabolic, Harris,
-             CompressedDipole):
+             CompressedDipole, Grid):
     _cls._device_class = _cls

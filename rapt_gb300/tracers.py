@@ -119,6 +119,7 @@ class Particle(_Pickle):
         """Particle.advance (Particle.py:230-309), on the GPU."""
         from . import Adiabatic
         res = advance_batch([self], delta)
+        _raise_if_left_grid(res)
         if self.check_adiabaticity and res["raised"][0]:
             raise Adiabatic
 
@@ -278,6 +279,7 @@ class GuidingCenter(_Pickle):
         """GuidingCenter.advance (GuidingCenter.py:397-458), on the GPU."""
         from . import NonAdiabatic
         res = advance_batch([self], delta, eom=eom)
+        _raise_if_left_grid(res)
         if self.check_adiabaticity and res["raised"][0]:
             raise NonAdiabatic
 
@@ -391,7 +393,7 @@ class Adaptive(_Pickle):
     def advance(self, delta):
         """Adaptive.advance (Adaptive.py:187-222), on the GPU."""
         assert self.trajlist[-1].check_adiabaticity
-        advance_batch([self], delta, verbose=True)
+        _raise_if_left_grid(advance_batch([self], delta, verbose=True))
 
     def _cat(self, name):
         return np.concatenate([np.asarray(getattr(p, name)(), float) for p in self.trajlist])
@@ -424,12 +426,19 @@ def _estimate_rows(kind, tracers, delta):
     return min(n, 4096) if kind == N.KIND_ADAPTIVE else n
 
 
+def _raise_if_left_grid(res):
+    # a Grid field evaluated outside its grid: the reference's interpolator raises
+    # ValueError from inside the step (fields.py:733-737); the rows before it stay
+    if res["status"] is not None and res["status"][0] == N.ST["OUT_OF_GRID"]:
+        raise ValueError("One of the requested xi is out of bounds: the tracer left the Grid field's grid")
+
+
 def advance_batch(tracers, delta, eom="TaoChanBrizardEOM", tableau=0, verbose=False):
     """Advance a list of tracers of one class sharing one field, in place, as if
     ``advance(delta)`` had been called on each. ``delta``: scalar or per tracer.
     Returns {"raised": bool array (Adiabatic / NonAdiabatic raised), "stats": ...}."""
     if len(tracers) == 0:
-        return {"raised": np.zeros(0, bool), "stats": None}
+        return {"raised": np.zeros(0, bool), "stats": None, "status": None}
     cls = type(tracers[0])
     field = tracers[0].field
     if any(type(t) is not cls or t.field is not field for t in tracers):

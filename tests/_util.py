@@ -7,12 +7,16 @@ from rapt_gb300 import fields as F
 
 def field_of(w):
     name, kw = w["field"]
+    if name == "SynthGrid":
+        return synth_grid(**kw)
     return getattr(F, name)(**kw)
 
 
 def oracle_field(O, w):
     name, kw = w["field"]
     fld = field_of(w)
+    if isinstance(fld, F.Grid):
+        return oracle_grid(O, fld)
     return O.field(name, fld.device_params())
 
 
@@ -91,3 +95,26 @@ def sensitivity_envelope(O, w, kind, delta, rel=1e-15, **over):
     n = 6 if kind == "particle" else 4
     pos, mom = rel_state_error(a["s"].T, b["s"], n)
     return a, pos, mom
+
+
+def synth_grid(times, static=True):
+    """Facade Grid over the synthetic snapshots of tests/golden/grid_data.py, by
+    the reference's recipe: a subclass whose parsefile returns a snapshot."""
+    from tests.golden import grid_data as GD
+
+    class SynthGrid(F.Grid):
+        def __init__(self, times):
+            self._snaps = {"snap%d" % k: g for k, g in enumerate(GD.snapshots(times))}
+            F.Grid.__init__(self, list(self._snaps))
+
+        def parsefile(self, filename):
+            return self._snaps[filename]
+
+    g = SynthGrid(times)
+    g.static = static
+    return g
+
+
+def oracle_grid(O, g):
+    """The oracle's copy of a facade Grid."""
+    return O.grid_field(g._t, g._x, g._y, g._z, g._B, g._E, static=g.static)
