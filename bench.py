@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="gc_doubledipole_1M",
-                    choices=["gc_doubledipole_1M", "harris_adaptive_262k", "earthdipole_particles", "compressed_adaptive"],
+                    choices=["gc_doubledipole_1M", "harris_adaptive_262k", "earthdipole_particles", "compressed_adaptive",
+                             "gc_grid_262k"],
                     help="gc_doubledipole_1M: the headline metric; harris_adaptive_262k: the batching comparison; "
                          "earthdipole_particles (config 4) and compressed_adaptive (config 5): form comparisons "
                          "on --n tracers")
@@ -467,6 +468,90 @@ def run_forms_workload(args, rank, ws, dist):
                       "kind": kind, "sim_tracer_seconds": sim, "results": res}), flush=True)
 
 
+def grid_cpu_baseline(g, w, n_sample, threads):
+    """The oracle on a sample of the gridded-field guiding centres, 1 s each."""
+    from oracle import oracle as O
+    idx = np.linspace(0, len(w["mass"]) - 1, n_sample).astype(np.int64)
+    f = O.grid_field(g._t, g._x, g._y, g._z, g._B, g._E, static=g.static)
+    p = w["params"]
+    cfg = O.config(rtol=p["rtol"], atol=p["atol"], gctimestep=p["gctimestep"])
+    tr = O.tracers_from_structs([O.gc_new_pa(f, w["pos"][i], w["v"][i], w["pa"][i], w["t0"], w["mass"][i],
+                                             w["charge"][i]) for i in idx])
+    t = time.perf_counter()
+    O.batch_advance(f, cfg, 1, tr, 1.0, nthreads=threads)
+    dt = time.perf_counter() - t
+    acc = int(tr["naccept"].sum())
+    return acc / dt, acc, dt
+
+
+def run_grid_workload(args, rank, ws, dist):
+    """Guiding centres in a gridded field (Grid, fields.py:513-814): 262,144
+    electrons in a 241 x 241 x 121 x 3-snapshot dipole grid (1.0 GB of B and E
+    resident in HBM), GuidingCenter.advance(1.0) per step, plain FP64 and FP32
+    forms; accepted steps/s against the oracle on host cores."""
+    from rapt_gb300 import Ensemble, workloads as W, _native as N
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx = N.Context(dev)
+    n = args.n if args.n != (1 << 20) else (1 << 18)
+    w = W.gc_grid(n, seed=rank)
+    t_build = time.perf_counter()
+    g = W.dipole_grid()
+    t_build = time.perf_counter() - t_build
+    ens = Ensemble(g, n, max_rows=8, ctx=ctx)
+    ens.configure(**w["params"])
+    ens.set_guiding_centers(w["pos"], w["v"], pa=w["pa"], t0=w["t0"], mass=w["mass"], charge=w["charge"])
+    init = {k: v.copy() for k, v in ens.h.items()}
+    steps, warmup = min(args.steps, 12), max(3, min(args.warmup, 6))  # the snapshots span 20 s
+    res = {}
+    clk = Clocks(dev) if rank == 0 else None
+    for name, form in (("plain", 0), ("fp32", 1)):
+        for k, v in init.items():
+            ens.h[k][...] = v
+        ens.upload()
+        ens.configure(form=form)
+        for _ in range(warmup):
+            ens.advance("gc", 1.0)
+            ens.rows(reset=True)
+        barrier(dist)
+        acc = rej = launches = 0
+        dev_ms = 0.0
+        for _ in range(steps):
+            st = ens.advance("gc", 1.0)
+            acc += st["accepted"]
+            rej += st["rejected"]
+            dev_ms += st["kernel_ms"]
+            launches += st["kernel_launches"]
+            ens.rows(reset=True)
+        barrier(dist)
+        h = ens.download()
+        dev_s = allmax(dist, dev_ms * 1e-3)
+        res[name] = {"accepted_per_s": allsum(dist, acc) / dev_s, "ms_per_step": dev_s * 1e3 / steps,
+                     "accepted": int(acc), "rejected": int(rej), "reject_rate": rej / max(acc, 1),
+                     "tracer_seconds_per_s": allsum(dist, float(n * steps)) / dev_s,
+                     "kernel_launches": int(launches),
+                     "status_counts": {int(k): int(v) for k, v in zip(*np.unique(h["status"], return_counts=True))}}
+    clocks = clk.stop() if clk else None
+    if rank != 0:
+        return
+    grid_bytes = int(g._B.nbytes + (g._E.nbytes if g._E is not None else 0))
+    line = {"metric": "accepted RK steps/s, guiding centres in a gridded field", "workload": "gc_grid_262k",
+            "value": res["plain"]["accepted_per_s"], "unit": UNIT, "n_gpus": ws, "steps": steps, "warmup": warmup,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded, config-2 distributions; "
+            "gridded dipole with E, 3 snapshots)",
+            "config": {"workload": "gc_grid_262k", "tracers_per_gpu": n, "grid": list(g._B.shape[:4]),
+                       "grid_bytes": grid_bytes, "gctimestep": 0.5, "rtol": w["params"]["rtol"],
+                       "atol": w["params"]["atol"],
+                       "static": False, "grid_build_s": t_build,
+                       "l2": "grid 1.0 GB > L2; tracers spread over it"},
+            "forms": res, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        n_s = args.cpu_sample or 2048
+        v, a, dt = grid_cpu_baseline(g, w, n_s, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": "%d of the %d tracers, 1 s each (%.1f s)" % (n_s, n, dt)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, ws, dist = dist_init(args)
@@ -476,6 +561,8 @@ def main():
         run_config3(args, rank, ws, dist)
     elif args.workload in ("earthdipole_particles", "compressed_adaptive"):
         run_forms_workload(args, rank, ws, dist)
+    elif args.workload == "gc_grid_262k":
+        run_grid_workload(args, rank, ws, dist)
     else:
         run_ours(args, rank, ws, dist)
     if dist is not None:

@@ -118,6 +118,7 @@ void attach_grid(const FieldP& g, FieldP* f) {
   f->gt = g.gt; f->gx = g.gx; f->gy = g.gy; f->gz = g.gz;
   f->gB = g.gB; f->gE = g.gE;
   f->nt = g.nt; f->nx = g.nx; f->ny = g.ny; f->nz = g.nz;
+  for (int a = 0; a < 4; ++a) f->ginv[a] = g.ginv[a];
 }
 
 void finish_field(FieldP* f) {
@@ -365,6 +366,10 @@ int rapt_grid_set(void* ctx, int32_t nt, const double* t, int32_t nx, const doub
   g.gB = dB; g.gE = dE;
   g.gt = da; g.gx = da + nt; g.gy = da + nt + nx; g.gz = da + nt + nx + ny;
   g.nt = nt; g.nx = nx; g.ny = ny; g.nz = nz;
+  // cell guesses of uniform axes (checked on the device against the axis values)
+  const double* ax[4] = {t, x, y, z};
+  const int an[4] = {nt, nx, ny, nz};
+  for (int a = 0; a < 4; ++a) g.ginv[a] = an[a] > 1 ? (an[a] - 1) / (ax[a][an[a] - 1] - ax[a][0]) : 0.0;
   build_field(RAPT_GRID, nullptr, 0, &c->field);
   attach_grid(g, &c->field);
   finish_field(&c->field);

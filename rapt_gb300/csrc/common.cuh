@@ -30,6 +30,7 @@ struct FieldP {
   // RAPT_GRID: axes and [nt][nx][ny][nz][3] snapshots resident on the device
   const double *gt, *gx, *gy, *gz;
   const double *gB, *gE;  // gE null: zero electric field
+  double ginv[4];         // (n - 1) / (g[n-1] - g[0]) per axis (t, x, y, z): the cell guess
   int nt, nx, ny, nz;
 };
 

@@ -179,79 +179,173 @@ struct GridV {
   double a, b, c;
 };
 
-// Cell index and normalised distance on a strictly ascending axis; v in [g[0], g[n-1]].
-__device__ __forceinline__ int grid_cell(const double* __restrict__ g, int n, double v, double& w) {
-  int lo = 0, hi = n - 1;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (__ldg(g + mid) <= v) lo = mid;
-    else hi = mid;
+// Cell index and normalised distance on a strictly ascending axis, v in
+// [g[0], g[n-1]]: the cell of a uniform axis is guessed from inv = (n-1) /
+// (g[n-1] - g[0]) and checked against the axis values (so the cell is exactly
+// the one SciPy's search finds); a wrong guess (non-uniform axis) falls back to
+// a binary search.
+__device__ __forceinline__ int grid_cell(const double* __restrict__ g, int n, double inv, double v, double& w) {
+  const double g0 = __ldg(g);
+  int i = min(max((int)((v - g0) * inv), 0), n - 2);
+  double lo = __ldg(g + i), hi = __ldg(g + i + 1);
+  if (!(lo <= v && (v < hi || i == n - 2))) {
+    int a = 0, b = n - 1;
+    while (b - a > 1) {
+      const int mid = (a + b) >> 1;
+      if (__ldg(g + mid) <= v) a = mid;
+      else b = mid;
+    }
+    i = a;
+    lo = __ldg(g + i);
+    hi = __ldg(g + i + 1);
   }
-  const double g0 = __ldg(g + lo);
-  w = (v - g0) / (__ldg(g + lo + 1) - g0);
-  return lo;
+  w = (v - lo) / (hi - lo);
+  return i;
 }
 
 __device__ __forceinline__ bool grid_inside(const double* __restrict__ g, int n, double v) {
   return __ldg(g) <= v && v <= __ldg(g + n - 1);
 }
 
-// One interpolation of a [nt][nx][ny][nz][3] array: not inlined, so that the
-// seven B evaluations of a guiding-centre right-hand side share one copy.
-static __device__ __noinline__ GridV grid_interp(const double* __restrict__ gt, const double* __restrict__ gx,
-                                                 const double* __restrict__ gy, const double* __restrict__ gz,
-                                                 const double* __restrict__ V, int nt, int nx, int ny, int nz,
-                                                 double t, double x, double y, double z) {
-  const double qnan = __longlong_as_double(0x7ff8000000000000LL);
-  if (!grid_inside(gx, nx, x) || !grid_inside(gy, ny, y) || !grid_inside(gz, nz, z) ||
-      (nt > 1 && !grid_inside(gt, nt, t)))
-    return GridV{qnan, qnan, qnan};
-  double wx, wy, wz, wt = 1.0;
-  const int ix = grid_cell(gx, nx, x, wx);
-  const int iy = grid_cell(gy, ny, y, wy);
-  const int iz = grid_cell(gz, nz, z, wz);
-  int it = 0;
-  if (nt > 1) it = grid_cell(gt, nt, t, wt);
-  const int64_t sy = nz, sx = (int64_t)ny * nz, st = (int64_t)nx * sx;
-  // one snapshot: weights (1 * wx) * wy * wz, the same products as the 3-D
-  // interpolator's, since 1 * w == w
-  const int ntc = nt > 1 ? 2 : 1;
-  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-  for (int ct = 0; ct < ntc; ++ct) {
-    const double w1 = ntc == 1 ? 1.0 : (ct ? wt : 1.0 - wt);
+struct GridCell {
+  int64_t base;          // node index of the lower corner at the lower snapshot
+  int64_t sx, sy, st;    // node strides
+  double wt, wx, wy, wz;
+  int ntc;               // time corners: 1 (one snapshot) or 2
+  bool ok;
+};
+
+__device__ __forceinline__ GridCell grid_locate(const double* __restrict__ gt, const double* __restrict__ gx,
+                                                const double* __restrict__ gy, const double* __restrict__ gz,
+                                                const double* inv, int nt, int nx, int ny, int nz, double t, double x,
+                                                double y, double z) {
+  GridCell c;
+  c.ok = grid_inside(gx, nx, x) && grid_inside(gy, ny, y) && grid_inside(gz, nz, z) &&
+         (nt == 1 || grid_inside(gt, nt, t));
+  c.sy = nz; c.sx = (int64_t)ny * nz; c.st = (int64_t)nx * c.sx;
+  c.ntc = nt > 1 ? 2 : 1;
+  c.wt = 1.0;
+  c.base = 0;
+  if (!c.ok) return c;
+  const int ix = grid_cell(gx, nx, inv[1], x, c.wx);
+  const int iy = grid_cell(gy, ny, inv[2], y, c.wy);
+  const int iz = grid_cell(gz, nz, inv[3], z, c.wz);
+  const int it = nt > 1 ? grid_cell(gt, nt, inv[0], t, c.wt) : 0;
+  c.base = it * c.st + ix * c.sx + iy * c.sy + iz;
+  return c;
+}
+
+// Corner sum of K arrays (3 components each) at one located point. One
+// snapshot: weights (1 * wx) * wy * wz, the same products as the 3-D
+// interpolator's, since 1 * w == w.
+template <int K>
+__device__ __forceinline__ void grid_sum(const GridCell& c, const double* const* V, double* out) {
+#pragma unroll
+  for (int k = 0; k < 3 * K; ++k) out[k] = 0.0;
+  for (int ct = 0; ct < c.ntc; ++ct) {
+    const double w1 = c.ntc == 1 ? 1.0 : (ct ? c.wt : 1.0 - c.wt);
 #pragma unroll
     for (int cx = 0; cx < 2; ++cx) {
-      const double w2 = __dmul_rn(w1, cx ? wx : 1.0 - wx);
+      const double w2 = __dmul_rn(w1, cx ? c.wx : 1.0 - c.wx);
 #pragma unroll
       for (int cy = 0; cy < 2; ++cy) {
-        const double w3 = __dmul_rn(w2, cy ? wy : 1.0 - wy);
-        const double* p = V + 3 * ((it + ct) * st + (ix + cx) * sx + (iy + cy) * sy + iz);
+        const double w3 = __dmul_rn(w2, cy ? c.wy : 1.0 - c.wy);
+        const int64_t node = c.base + ct * c.st + cx * c.sx + cy * c.sy;
 #pragma unroll
         for (int cz = 0; cz < 2; ++cz) {
-          const double w = __dmul_rn(w3, cz ? wz : 1.0 - wz);
-          s0 = __dadd_rn(s0, __dmul_rn(__ldg(p + 3 * cz + 0), w));
-          s1 = __dadd_rn(s1, __dmul_rn(__ldg(p + 3 * cz + 1), w));
-          s2 = __dadd_rn(s2, __dmul_rn(__ldg(p + 3 * cz + 2), w));
+          const double w = __dmul_rn(w3, cz ? c.wz : 1.0 - c.wz);
+#pragma unroll
+          for (int k = 0; k < K; ++k) {
+            const double* p = V[k] + 3 * (node + cz);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) out[3 * k + j] = __dadd_rn(out[3 * k + j], __dmul_rn(__ldg(p + j), w));
+          }
         }
       }
     }
   }
-  return GridV{s0, s1, s2};
+}
+
+// The device-resident grid as scalars, so that the non-inlined interpolation
+// functions take their arguments in registers.
+#define RAPT_GRID_ARGS                                                                                      \
+  const double *__restrict__ gt, const double *__restrict__ gx, const double *__restrict__ gy,              \
+      const double *__restrict__ gz, double it_, double ix_, double iy_, double iz_, int nt, int nx, int ny, \
+      int nz
+#define RAPT_GRID_PASS(f) \
+  f.gt, f.gx, f.gy, f.gz, f.ginv[0], f.ginv[1], f.ginv[2], f.ginv[3], f.nt, f.nx, f.ny, f.nz
+
+struct GridV6 {
+  double v[6];
+};
+
+// One interpolation of a [nt][nx][ny][nz][3] array: not inlined, so that the
+// evaluations of a guiding-centre right-hand side share one copy.
+static __device__ __noinline__ GridV grid_interp(RAPT_GRID_ARGS, const double* __restrict__ V, double t, double x,
+                                                 double y, double z) {
+  const double inv[4] = {it_, ix_, iy_, iz_};
+  const GridCell c = grid_locate(gt, gx, gy, gz, inv, nt, nx, ny, nz, t, x, y, z);
+  if (!c.ok) {
+    const double qnan = __longlong_as_double(0x7ff8000000000000LL);
+    return GridV{qnan, qnan, qnan};
+  }
+  const double* arr[1] = {V};
+  double o[3];
+  grid_sum<1>(c, arr, o);
+  return GridV{o[0], o[1], o[2]};
+}
+
+// B and E at one point from one cell search (the right-hand sides need both).
+static __device__ __noinline__ GridV6 grid_interp_BE(RAPT_GRID_ARGS, const double* __restrict__ VB,
+                                                     const double* __restrict__ VE, double t, double x, double y,
+                                                     double z) {
+  const double inv[4] = {it_, ix_, iy_, iz_};
+  const GridCell c = grid_locate(gt, gx, gy, gz, inv, nt, nx, ny, nz, t, x, y, z);
+  GridV6 r;
+  if (!c.ok) {
+    const double qnan = __longlong_as_double(0x7ff8000000000000LL);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) r.v[k] = qnan;
+    return r;
+  }
+  if (VE) {
+    const double* arr[2] = {VB, VE};
+    grid_sum<2>(c, arr, r.v);
+  } else {
+    const double* arr[1] = {VB};
+    grid_sum<1>(c, arr, r.v);
+    r.v[3] = r.v[4] = r.v[5] = 0.0;
+  }
+  return r;
 }
 
 template <>
 struct Field<RAPT_GRID> {
   static constexpr bool kStatic = false;  // the runtime flag f.is_static decides (field_static)
   __device__ __forceinline__ static void B(const FieldP& f, double t, double x, double y, double z, double* o) {
-    const GridV r = grid_interp(f.gt, f.gx, f.gy, f.gz, f.gB, f.nt, f.nx, f.ny, f.nz, t, x, y, z);
+    const GridV r = grid_interp(RAPT_GRID_PASS(f), f.gB, t, x, y, z);
     o[0] = r.a; o[1] = r.b; o[2] = r.c;
   }
   __device__ __forceinline__ static void E(const FieldP& f, double t, double x, double y, double z, double* o) {
     if (!f.gE) { o[0] = o[1] = o[2] = 0.0; return; }
-    const GridV r = grid_interp(f.gt, f.gx, f.gy, f.gz, f.gE, f.nt, f.nx, f.ny, f.nz, t, x, y, z);
+    const GridV r = grid_interp(RAPT_GRID_PASS(f), f.gE, t, x, y, z);
     o[0] = r.a; o[1] = r.b; o[2] = r.c;
   }
 };
+
+// B and E at one point: one cell search for a Grid, the two model functions otherwise.
+template <int M>
+__device__ __forceinline__ void field_BE(const FieldP& f, double t, double x, double y, double z, double* B,
+                                         double* E) {
+  if constexpr (M == RAPT_GRID) {
+    const GridV6 r = grid_interp_BE(RAPT_GRID_PASS(f), f.gB, f.gE, t, x, y, z);
+    B[0] = r.v[0]; B[1] = r.v[1]; B[2] = r.v[2];
+    E[0] = r.v[3]; E[1] = r.v[4]; E[2] = r.v[5];
+  } else {
+    Field<M>::B(f, t, x, y, z, B);
+    Field<M>::E(f, t, x, y, z, E);
+  }
+}
 
 // _Field.static (fields.py:41): fixed by the equations of the analytic models,
 // the runtime attribute for Grid (which leaves it True by default).

@@ -17,8 +17,7 @@ struct ParticleRHS {
     double igm = inv_gm_frozen;
     if (!field_static<M>(f)) igm = rsqrt(mass2 + (Y[3] * Y[3] + Y[4] * Y[4] + Y[5] * Y[5]) * (1.0 / (kC * kC)));
     double B[3], E[3];
-    Field<M>::B(f, t, Y[0], Y[1], Y[2], B);
-    Field<M>::E(f, t, Y[0], Y[1], Y[2], E);
+    field_BE<M>(f, t, Y[0], Y[1], Y[2], B, E);
     o[0] = Y[3] * igm;
     o[1] = Y[4] * igm;
     o[2] = Y[5] * igm;
@@ -47,8 +46,13 @@ struct GcRHS {
   __device__ __forceinline__ void operator()(double t, const double* Y, double* o) const {
     const double ppar = Y[3];
     double ub[3], Bmag;
-    double B[3];
-    Field<M>::B(f, t, Y[0], Y[1], Y[2], B);
+    double B[3], Eg[3];
+    if constexpr (M == RAPT_GRID) {  // one cell search for B and E
+      if (eom == 0) field_BE<M>(f, t, Y[0], Y[1], Y[2], B, Eg);
+      else Field<M>::B(f, t, Y[0], Y[1], Y[2], B);
+    } else {
+      Field<M>::B(f, t, Y[0], Y[1], Y[2], B);
+    }
     {
       const double b2 = dot3(B, B);
       const double ib = rsqrt(b2);
@@ -62,7 +66,8 @@ struct GcRHS {
       const double g2 = 1.0 + k_mu * Bmag + pm * pm;
       const double rg = rsqrt(g2);
       double E[3], db[3];
-      Field<M>::E(f, t, Y[0], Y[1], Y[2], E);
+      if constexpr (M == RAPT_GRID) { E[0] = Eg[0]; E[1] = Eg[1]; E[2] = Eg[2]; }
+      else Field<M>::E(f, t, Y[0], Y[1], Y[2], E);
       dbdt<M>(f, t, Y, db);
       const double pq = ppar * qinv;
       double Bs[3] = {B[0] + pq * cb[0], B[1] + pq * cb[1], B[2] + pq * cb[2]};
