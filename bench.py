@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="gc_doubledipole_1M",
                     choices=["gc_doubledipole_1M", "harris_adaptive_262k", "earthdipole_particles", "compressed_adaptive",
-                             "gc_grid_262k"],
+                             "gc_grid_262k", "gc_dense_cadence"],
                     help="gc_doubledipole_1M: the headline metric; harris_adaptive_262k: the batching comparison; "
                          "earthdipole_particles (config 4) and compressed_adaptive (config 5): form comparisons "
                          "on --n tracers")
@@ -552,6 +552,67 @@ def run_grid_workload(args, rank, ws, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_dense_workload(args, rank, ws, dist):
+    """Output cadence against cost: 262,144 config-2 electrons with rows every
+    0.01 s, GuidingCenter.advance(0.5) per step, the reference's restart per row
+    against dense output (one integration per advance, rows from the continuous
+    extension); simulated tracer-seconds/s and right-hand sides per
+    tracer-second of each, plain FP64."""
+    from rapt_gb300 import Ensemble, workloads as W, fields as F, _native as N
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx = N.Context(dev)
+    n = args.n if args.n != (1 << 20) else (1 << 18)
+    w = W.subsample(W.gc_bench(1 << 20, seed=rank), np.arange(0, 1 << 20, (1 << 20) // n)[:n])
+    cadence, span = 0.01, 0.5
+    # 50 rows per step, plus the 17 a dense-output step may cover
+    ens = Ensemble(F.DoubleDipole(), n, max_rows=128, ctx=ctx)
+    ens.configure(rtol=1e-8, atol=1e-8, gctimestep=cadence)
+    ens.set_guiding_centers(w["pos"], w["v"], pa=w["pa"], t0=0.0, mass=w["mass"], charge=w["charge"])
+    init = {k: v.copy() for k, v in ens.h.items()}
+    steps, warmup = args.steps, max(3, args.warmup)
+    res = {}
+    clk = Clocks(dev) if rank == 0 else None
+    for name, dense in (("restart", 0), ("dense", 1)):
+        for k, v in init.items():
+            ens.h[k][...] = v
+        ens.upload()
+        ens.configure(dense_output=dense)
+        for _ in range(warmup):
+            ens.advance("gc", span)
+            ens.rows(reset=True)
+        barrier(dist)
+        acc = rhs = launches = 0
+        dev_ms = 0.0
+        for _ in range(steps):
+            st = ens.advance("gc", span)
+            acc += st["accepted"]
+            rhs += st["rhs_evals"]
+            dev_ms += st["kernel_ms"]
+            launches += st["kernel_launches"]
+            ens.rows(reset=True)
+        barrier(dist)
+        h = ens.download()
+        dev_s = allmax(dist, dev_ms * 1e-3)
+        sim = allsum(dist, float(n * steps * span))
+        res[name] = {"tracer_seconds_per_s": sim / dev_s, "accepted_per_s": allsum(dist, acc) / dev_s,
+                     "ms_per_step": dev_s * 1e3 / steps, "rhs_per_tracer_second": rhs / (n * steps * span),
+                     "accepted": int(acc), "kernel_launches": int(launches),
+                     "failed": int(np.count_nonzero(h["status"])),
+                     "status_counts": {int(k): int(v) for k, v in zip(*np.unique(h["status"], return_counts=True))}}
+    clocks = clk.stop() if clk else None
+    if rank != 0:
+        return
+    line = {"metric": "simulated tracer-seconds/s at a 0.01 s output cadence", "workload": "gc_dense_cadence",
+            "value": res["dense"]["tracer_seconds_per_s"], "unit": "tracer-seconds/s", "n_gpus": ws,
+            "steps": steps, "warmup": warmup, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (seeded, config-2 distributions)",
+            "config": {"workload": "gc_dense_cadence", "tracers_per_gpu": n, "gctimestep": cadence,
+                       "step": "GuidingCenter.advance(0.5)", "rtol": 1e-8, "atol": 1e-8},
+            "results": res, "dense_vs_restart": res["dense"]["tracer_seconds_per_s"] /
+            res["restart"]["tracer_seconds_per_s"], "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, ws, dist = dist_init(args)
@@ -563,6 +624,8 @@ def main():
         run_forms_workload(args, rank, ws, dist)
     elif args.workload == "gc_grid_262k":
         run_grid_workload(args, rank, ws, dist)
+    elif args.workload == "gc_dense_cadence":
+        run_dense_workload(args, rank, ws, dist)
     else:
         run_ours(args, rank, ws, dist)
     if dist is not None:

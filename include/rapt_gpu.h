@@ -80,7 +80,8 @@ enum {
 enum {
   RAPT_FLAG_CHECK_ADIABATICITY = 1, /* tracer.check_adiabaticity */
   RAPT_FLAG_RAISED = 2,             /* out: Adiabatic / NonAdiabatic was raised */
-  RAPT_FLAG_DONE = 4                /* internal: advance finished for this call */
+  RAPT_FLAG_DONE = 4,               /* internal: advance finished for this call */
+  RAPT_FLAG_REJECTED = 8            /* internal: dense output, the last attempt was rejected */
 };
 
 /* Mirrors rapt.params (rapt/__init__.py:21-34) plus device options. */
@@ -110,6 +111,10 @@ typedef struct {
   double bounceresolution;       /* params["bounceresolution"]: with gctimestep == 0 the GC cadence is
                                     bounceperiod() / bounceresolution (GuidingCenter.py:443-446) */
   double fieldlineresolution;    /* params["fieldlineresolution"] (fieldline.py:31-35) */
+  int32_t dense_output;          /* 1: guiding centres integrate through each advance() call without restarting
+                                    at the output times (step <= the cadence) and output rows from DOPRI5's
+                                    order-4 continuous extension; plain form, DOPRI5 only. No reference
+                                    counterpart (the reference restarts SciPy's dopri5 per row) */
 } rapt_config;
 
 /* Host-side SoA view of an ensemble. Any pointer may be NULL on download to

@@ -41,7 +41,7 @@ class Config(C.Structure):
                 ("gctimestep", C.c_double), ("epss", C.c_double), ("epst", C.c_double),
                 ("enforce_equatorial", C.c_int), ("tableau", C.c_int), ("gc_eom", C.c_int),
                 ("nsteps", C.c_int), ("rkf_tol", C.c_double), ("rkf_hmin", C.c_double),
-                ("bounceres", C.c_double), ("flres", C.c_double), ("bounce_quad", C.c_int)]
+                ("bounceres", C.c_double), ("flres", C.c_double), ("bounce_quad", C.c_int), ("dense", C.c_int)]
 
 
 TRACER_DTYPE = np.dtype([
@@ -154,10 +154,10 @@ def grid_field(t, x, y, z, B, E=None, static=True):
 
 def config(rtol=1.49012e-8, atol=1.49012e-8, cycres=10, gctimestep=0.0, epss=5e-2, epst=5e-2,
            enforce_equatorial=False, tableau=0, gc_eom=0, nsteps=500, rkf_tol=1e-3,
-           rkf_hmin=1e-12, bounceres=10, flres=50, bounce_quad=0):
+           rkf_hmin=1e-12, bounceres=10, flres=50, bounce_quad=0, dense=0):
     c = Config()
     lib().orc_config_default(C.byref(c))
-    c.bounceres, c.flres, c.bounce_quad = bounceres, flres, bounce_quad
+    c.bounceres, c.flres, c.bounce_quad, c.dense = bounceres, flres, bounce_quad, int(dense)
     c.rtol, c.atol, c.cycres, c.gctimestep = rtol, atol, cycres, gctimestep
     c.epss, c.epst, c.enforce_equatorial = epss, epst, int(bool(enforce_equatorial))
     c.tableau, c.gc_eom, c.nsteps, c.rkf_tol, c.rkf_hmin = tableau, gc_eom, nsteps, rkf_tol, rkf_hmin

@@ -1034,12 +1034,139 @@ int orc_particle_advance(const orc_field* f, const orc_config* c, orc_tracer* p,
   return 0;
 }
 
+// Dense-output guiding-centre advance (no reference counterpart; the option
+// rapt_config.dense_output of the GPU library): one DOPRI5 integration through
+// the whole call with hmax = 16 output intervals, rows at the reference's output times from the
+// order-4 continuous extension of the step that covers each (Hairer, Norsett &
+// Wanner, Solving ODEs I, II.6, the DOPRI5 code's CONTD5 coefficients), the
+// adiabaticity check on each row, and the call ending in the last row's state.
+static int gc_advance_dense(const orc_field* f, const orc_config* c, orc_tracer* g, double delta, double dt,
+                            int check_adiabaticity, double* rows, int max_rows, int* nrows) {
+  const double a21 = 0.2, a31 = 3.0 / 40.0, a32 = 9.0 / 40.0;
+  const double a41 = 44.0 / 45.0, a42 = -56.0 / 15.0, a43 = 32.0 / 9.0;
+  const double a51 = 19372.0 / 6561.0, a52 = -25360.0 / 2187.0, a53 = 64448.0 / 6561.0, a54 = -212.0 / 729.0;
+  const double a61 = 9017.0 / 3168.0, a62 = -355.0 / 33.0, a63 = 46732.0 / 5247.0, a64 = 49.0 / 176.0,
+               a65 = -5103.0 / 18656.0;
+  const double a71 = 35.0 / 384.0, a73 = 500.0 / 1113.0, a74 = 125.0 / 192.0, a75 = -2187.0 / 6784.0,
+               a76 = 11.0 / 84.0;
+  const double e1 = 71.0 / 57600.0, e3 = -71.0 / 16695.0, e4 = 71.0 / 1920.0, e5 = -17253.0 / 339200.0,
+               e6 = 22.0 / 525.0, e7 = -1.0 / 40.0;
+  const double d1 = -12715105075.0 / 11282082432.0, d3 = 87487479700.0 / 32700410799.0,
+               d4 = -10690763975.0 / 1880347072.0, d5 = 701980252875.0 / 199316789632.0,
+               d6 = -1453857185.0 / 822651844.0, d7 = 69997945.0 / 29380423.0;
+  const double beta = 0.04, safe = 0.9, expo1 = 0.2 - beta * 0.75, facc1 = 5.0, facc2 = 0.1;
+  const double uround = 2.3e-16;
+  auto F = [&](double t, const double* Y, double* o) {
+    orc_gc_rhs(f, c, c->gc_eom, g->mass, g->charge, g->mu, g->v, t, Y, o);
+  };
+  const int n = 4;
+  const double stop = g->t + delta;
+  double t_row = g->t, rt = g->t, y[4], k1[4];
+  std::memcpy(y, g->s, sizeof(y));
+  if (!(t_row < stop)) return 0;
+  F(rt, y, k1);
+  const double hmax = 16 * dt;
+  double h = hinit(F, n, rt, y, 1.0, k1, 5, hmax, c->atol, c->rtol);
+  g->nfcn += 2;
+  double facold = 1e-4;
+  bool reject = false;
+  int nst = 0;
+  for (int64_t guard = 0; guard < 100000000; ++guard) {
+    if (nst > c->nsteps || 0.1 * std::fabs(h) <= std::fabs(rt) * uround) {
+      g->status = nst > c->nsteps ? ORC_ST_MAXSTEPS : ORC_ST_HMIN;
+      g->t = rt; g->tcur = rt;
+      std::memcpy(g->s, y, sizeof(y));
+      put_row(rows, max_rows, nrows, rt, y, 4);
+      return 0;
+    }
+    ++nst;
+    g->nstep++;
+    double k2[4], k3[4], k4[4], k5[4], k6[4], k7[4], y1[4], yt[4];
+    for (int i = 0; i < n; ++i) yt[i] = y[i] + h * (a21 * k1[i]);
+    F(rt + 0.2 * h, yt, k2);
+    for (int i = 0; i < n; ++i) yt[i] = y[i] + h * (a31 * k1[i] + a32 * k2[i]);
+    F(rt + 0.3 * h, yt, k3);
+    for (int i = 0; i < n; ++i) yt[i] = y[i] + h * (a41 * k1[i] + a42 * k2[i] + a43 * k3[i]);
+    F(rt + 0.8 * h, yt, k4);
+    for (int i = 0; i < n; ++i) yt[i] = y[i] + h * (a51 * k1[i] + a52 * k2[i] + a53 * k3[i] + a54 * k4[i]);
+    F(rt + (8.0 / 9.0) * h, yt, k5);
+    for (int i = 0; i < n; ++i)
+      yt[i] = y[i] + h * (a61 * k1[i] + a62 * k2[i] + a63 * k3[i] + a64 * k4[i] + a65 * k5[i]);
+    F(rt + h, yt, k6);
+    for (int i = 0; i < n; ++i) y1[i] = y[i] + h * (a71 * k1[i] + a73 * k3[i] + a74 * k4[i] + a75 * k5[i] + a76 * k6[i]);
+    F(rt + h, y1, k7);
+    g->nfcn += 6;
+    double err = 0, dd[4];
+    for (int i = 0; i < n; ++i) {
+      const double ei = (e1 * k1[i] + e3 * k3[i] + e4 * k4[i] + e5 * k5[i] + e6 * k6[i] + e7 * k7[i]) * h;
+      const double sk = c->atol + c->rtol * std::max(std::fabs(y[i]), std::fabs(y1[i]));
+      err += (ei / sk) * (ei / sk);
+      dd[i] = h * (d1 * k1[i] + d3 * k3[i] + d4 * k4[i] + d5 * k5[i] + d6 * k6[i] + d7 * k7[i]);
+    }
+    err = std::sqrt(err / n);
+    if (f->model == ORC_GRID && std::isnan(err)) {  // the reference raises ValueError: no row
+      g->status = ORC_ST_OUT_OF_GRID;
+      return 0;
+    }
+    const double fac11 = std::pow(err, expo1);
+    double fac = fac11 / std::pow(facold, beta);
+    fac = std::max(facc2, std::min(facc1, fac / safe));
+    double hnew = h / fac;
+    if (err <= 1.0) {
+      facold = std::max(err, 1.0e-4);
+      g->naccept++;
+      const double told = rt, hs = h;
+      rt = rt + h;
+      if (std::fabs(hnew) > hmax) hnew = hmax;
+      if (reject) hnew = std::min(std::fabs(hnew), std::fabs(h));
+      reject = false;
+      h = hnew;
+      for (int r = 0; r <= 16; ++r) {
+        const double tn = t_row + dt;
+        if (!(tn <= rt)) break;
+        const double th = (tn - told) / hs, th1 = 1.0 - th;
+        double yr[4];
+        for (int i = 0; i < n; ++i) {
+          const double ydiff = y1[i] - y[i];
+          const double bspl = hs * k1[i] - ydiff;
+          const double r4 = ydiff - hs * k7[i] - bspl;
+          yr[i] = y[i] + th * (ydiff + th1 * (bspl + th * (r4 + th1 * dd[i])));
+        }
+        t_row = tn;
+        nst = 0;
+        put_row(rows, max_rows, nrows, tn, yr, 4);
+        g->t = tn; g->tcur = tn;
+        std::memcpy(g->s, yr, sizeof(yr));
+        if (check_adiabaticity && finite_n(yr, 4) && !orc_gc_isadiabatic(f, c, g)) return 1;
+        if (!(t_row < stop)) {
+          if (!finite_n(yr, 4)) g->status = ORC_ST_NONFINITE;
+          return 0;
+        }
+      }
+      std::memcpy(k1, k7, sizeof(k1));
+      std::memcpy(y, y1, sizeof(y));
+      if (!finite_n(y, 4)) {
+        g->status = ORC_ST_NONFINITE;
+        return 0;
+      }
+    } else {
+      hnew = h / std::min(facc1, fac11 / safe);
+      reject = true;
+      g->nreject++;
+      h = hnew;
+    }
+  }
+  g->status = ORC_ST_MAXSTEPS;
+  return 0;
+}
+
 int orc_gc_advance(const orc_field* f, const orc_config* c, orc_tracer* g, double delta,
                    int check_adiabaticity, double* rows, int max_rows, int* nrows) {
   // GuidingCenter.advance, rapt/GuidingCenter.py:397-458 (dopri5 at :450)
   // cadence: GCtimestep, or the bounce period at the current state / bounceresolution (:443-446)
   const double dt = c->gctimestep != 0 ? c->gctimestep : orc_gc_bounceperiod(f, g, c->flres, c->bounce_quad) / c->bounceres;
   if (!(dt > 0) || !std::isfinite(dt)) { g->status = ORC_ST_BAD_INPUT; return 0; }
+  if (c->dense) return gc_advance_dense(f, c, g, delta, dt, check_adiabaticity, rows, max_rows, nrows);
   const double t0 = g->t;
   double rt = g->t;
   double y[4];

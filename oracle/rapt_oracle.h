@@ -55,6 +55,7 @@ typedef struct {
   double bounceres;        /* params["bounceresolution"]: GC cadence T_b / bounceres when gctimestep == 0 */
   double flres;            /* params["fieldlineresolution"] */
   int bounce_quad;         /* half-bounce integral: 0 QAGS as the reference, 1 converged */
+  int dense;               /* guiding centres: dense output without restarts (no reference counterpart) */
 } orc_config;
 
 /* One tracer (a Particle or a GuidingCenter segment). */

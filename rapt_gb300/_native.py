@@ -34,7 +34,8 @@ class RaptConfig(C.Structure):
                 ("max_steps_per_launch", C.c_int64), ("blocks_per_sm", C.c_int32),
                 ("use_graph", C.c_int32), ("collect", C.c_int32), ("learned_scale", C.c_double),
                 ("learned_every", C.c_int32), ("per_tracer_launches", C.c_int32),
-                ("bounceresolution", C.c_double), ("fieldlineresolution", C.c_double)]
+                ("bounceresolution", C.c_double), ("fieldlineresolution", C.c_double),
+                ("dense_output", C.c_int32)]
 
 
 class RaptHostState(C.Structure):

@@ -85,7 +85,7 @@ size_t ensemble_bytes(int64_t n, int max_rows, int max_sw) {
   b += 2 * al(N);                                      // mode, seg_active
   b += al(N * max_rows) + al(N * max_sw);              // row_mode, sw_mode
   b += 5 * al(N * 4);                                  // status, flags, nrows, nswitch, nseg
-  b += 19 * al(N * 8);                                 // doubles
+  b += 22 * al(N * 8);                                 // doubles
   b += al(N * max_rows * 7 * 8) + al(N * max_sw * 8);  // rows, sw_time
   b += 3 * al(N * 8);                                  // int64 counters
   return b;
@@ -393,6 +393,8 @@ int rapt_config_set(void* ctx, const rapt_config* g) {
   if (!(g->learned_scale >= 0)) return fail(c, RAPT_ERR_INVALID, "learned_scale must be >= 0");
   if (g->learned_every < 0) return fail(c, RAPT_ERR_INVALID, "learned_every must be >= 0");
   if (!(g->gctimestep >= 0)) return fail(c, RAPT_ERR_INVALID, "GCtimestep must be >= 0");
+  if (g->dense_output && (g->form != RAPT_FORM_PLAIN || g->tableau != 0 || g->collect))
+    return fail(c, RAPT_ERR_UNSUPPORTED, "dense output runs the plain FP64 DOPRI5 guiding-centre kernel");
   if (g->gctimestep == 0 && !(g->bounceresolution > 0 && g->fieldlineresolution > 0))
     return fail(c, RAPT_ERR_INVALID, "bounceresolution and fieldlineresolution must be > 0");
   c->cfg = *g;
@@ -439,6 +441,9 @@ int rapt_ensemble_alloc(void* ctx, int64_t n, int32_t max_rows, int32_t max_swit
   E.seg_stop = carve<double>(p, N);
   E.seg_dt = carve<double>(p, N);
   E.seg_gm = carve<double>(p, N);
+  E.carry_h = carve<double>(p, N);
+  E.carry_fac = carve<double>(p, N);
+  E.carry_nst = carve<double>(p, N);
   E.rows = carve<double>(p, N * max_rows * 7);
   E.sw_time = carve<double>(p, N * max_switch);
   E.naccept = carve<int64_t>(p, N);
@@ -557,6 +562,7 @@ static DevEnsemble ensemble_view(const DevEnsemble& E, int64_t k, int max_rows, 
   V.mu += k; V.v += k; V.mass += k; V.charge += k;
   V.naccept += k; V.nreject += k; V.nfcn += k; V.nswitch += k;
   V.delta += k; V.seg_stop += k; V.seg_dt += k; V.seg_gm += k; V.seg_active += k; V.nseg += k;
+  V.carry_h += k; V.carry_fac += k; V.carry_nst += k;
   V.rows += (size_t)k * max_rows * 7;
   V.row_mode += (size_t)k * max_rows;
   V.nrows += k;
@@ -612,7 +618,11 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
     return fail(c, RAPT_ERR_STATE, "collection without a sample buffer (rapt_mlp_samples_reserve)");
   // the step learner drives the guiding-centre kernels; particles run the plain controller
   int bps_p = f32 ? T.occ_particle32(block) : T.occ_particle[tab](block);
-  int bps_g = tab != 0 ? T.occ_gc[tab](block) : (f32 ? T.occ_gc32_lrn[lrn](block) : T.occ_gc_lrn[lrn](block));
+  const bool dense = c->cfg.dense_output != 0;
+  if (dense && kind != RAPT_KIND_PARTICLE && c->max_rows < 18)
+    return fail(c, RAPT_ERR_INVALID, "dense output needs max_rows >= 18 (a step may cover 17 output times)");
+  int bps_g = dense ? T.occ_gc_dense(block)
+                    : (tab != 0 ? T.occ_gc[tab](block) : (f32 ? T.occ_gc32_lrn[lrn](block) : T.occ_gc_lrn[lrn](block)));
   if (c->cfg.blocks_per_sm > 0) {
     bps_p = std::min(bps_p, c->cfg.blocks_per_sm);
     bps_g = std::min(bps_g, c->cfg.blocks_per_sm);
@@ -655,7 +665,7 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
     }
     if (kind != RAPT_KIND_PARTICLE) {
       a.grid = grid_g;
-      CK(tab != 0 ? T.gc[tab](a) : (f32 ? T.gc32_lrn[lrn](a) : T.gc_lrn[lrn](a)));
+      CK(dense ? T.gc_dense(a) : (tab != 0 ? T.gc[tab](a) : (f32 ? T.gc32_lrn[lrn](a) : T.gc_lrn[lrn](a))));
       ++kl;
     }
     return RAPT_OK;

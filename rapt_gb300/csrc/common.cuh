@@ -83,6 +83,11 @@ struct DevEnsemble {
   double* seg_stop;    // t0 + delta of the current tracer.advance() call
   double* seg_dt;      // output cadence of the current call
   double* seg_gm;      // gamma*m frozen at the start of a Particle.advance call
+  // dense-output guiding-centre integration carried between steps and launches:
+  // step size (0: not started), facold, steps since the last row
+  double* carry_h;
+  double* carry_fac;
+  double* carry_nst;
   int8_t* seg_active;  // 1 while a tracer.advance() call is in progress
   int32_t* nseg;       // advance() calls made by Adaptive in this call
   // outputs

@@ -1,5 +1,6 @@
 // inst_body.cuh -- instantiates every kernel for one field model. Included by
 // inst_model<k>.cu with RAPT_MODEL defined, so the models compile in parallel.
+#include "dense_kernels.cuh"
 #include "eval_kernels.cuh"
 #include "fp32_kernels.cuh"
 #include "launch.h"
@@ -31,6 +32,15 @@ template <int TAB>
 int occ_gc(int block) {
   int nb = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc<kM, TAB>, block, 0);
+  return nb;
+}
+cudaError_t launch_gc_dense(const LaunchArgs& a) {
+  k_gc_dense<kM><<<a.grid, a.block, 0, a.stream>>>(a.E, a.P, a.S);
+  return cudaGetLastError();
+}
+int occ_gc_dense(int block) {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gc_dense<kM>, block, 0);
   return nb;
 }
 cudaError_t launch_particle32(const LaunchArgs& a) {
@@ -133,5 +143,7 @@ void RAPT_CAT(register_model_, RAPT_MODEL)(ModelTable* t) {
   t->rhs_eval = rhs_eval;
   t->adaptive_init = adaptive_init;
   t->bounce_period = bounce_period;
+  t->gc_dense = launch_gc_dense;
+  t->occ_gc_dense = occ_gc_dense;
 }
 }  // namespace rapt

@@ -38,6 +38,8 @@ struct ModelTable {
   RhsEvalFn rhs_eval;
   AdaptiveInitFn adaptive_init;
   BounceFn bounce_period;
+  LaunchFn gc_dense;  // DOPRI5 guiding centres with dense output (rapt_config.dense_output)
+  OccFn occ_gc_dense;
 };
 
 // MLP kernels (mlp.cu); packed BF16 weights take kMlpPackedWords u32

@@ -21,6 +21,11 @@ constexpr double a71 = 35.0 / 384.0, a73 = 500.0 / 1113.0, a74 = 125.0 / 192.0, 
                  a76 = 11.0 / 84.0;
 constexpr double e1 = 71.0 / 57600.0, e3 = -71.0 / 16695.0, e4 = 71.0 / 1920.0, e5 = -17253.0 / 339200.0,
                  e6 = 22.0 / 525.0, e7 = -1.0 / 40.0;
+// continuous extension of order 4 (Hairer, Norsett & Wanner, Solving ODEs I, II.6;
+// the coefficients of the DOPRI5 code's dense output)
+constexpr double d1 = -12715105075.0 / 11282082432.0, d3 = 87487479700.0 / 32700410799.0,
+                 d4 = -10690763975.0 / 1880347072.0, d5 = 701980252875.0 / 199316789632.0,
+                 d6 = -1453857185.0 / 822651844.0, d7 = 69997945.0 / 29380423.0;
 }  // namespace dp5
 
 namespace dp8 {
@@ -156,10 +161,10 @@ static __constant__ double kDp5C[7] = {0, dp5::c2, dp5::c3, dp5::c4, dp5::c5, 1.
 // that an expensive right-hand side (the guiding-centre stencil) is emitted once
 // rather than six times; stage sums run over all earlier slopes with zero
 // coefficients where the tableau has none.
-template <int NV, class F>
+template <int NV, class F, bool DENSE = false>
 __device__ __forceinline__ void dopri5_attempt_rolled(const F& f, double x, const double* y, const double* k1,
                                                       double h, double rtol, double atol, double* y1, double* k7,
-                                                      double& err) {
+                                                      double& err, double* dd = nullptr) {
   using namespace dp5;
   double k2[NV], k3[NV], k4[NV], k5[NV], k6[NV], yt[NV], kt[NV];
 #pragma unroll
@@ -188,8 +193,25 @@ __device__ __forceinline__ void dopri5_attempt_rolled(const F& f, double x, cons
     const double sk = atol + rtol * fmax(fabs(y[i]), fabs(y1[i]));
     const double r = ei / sk;
     e += r * r;
+    if (DENSE) dd[i] = h * (d1 * k1[i] + d3 * k3[i] + d4 * k4[i] + d5 * k5[i] + d6 * k6[i] + d7 * k7[i]);
   }
   err = sqrt(e * (1.0 / NV));
+}
+
+// DOPRI5 continuous extension at theta in [0, 1] of an accepted step from y0
+// (slope k1) to y1 (slope k7): the Hermite-like form of Hairer's CONTD5 with
+// the fifth coefficient dd from the attempt.
+template <int NV>
+__device__ __forceinline__ void dopri5_dense(const double* y0, const double* y1, const double* k1, const double* k7,
+                                             const double* dd, double h, double theta, double* out) {
+  const double th1 = 1.0 - theta;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const double ydiff = y1[i] - y0[i];
+    const double bspl = h * k1[i] - ydiff;
+    const double r4 = ydiff - h * k7[i] - bspl;
+    out[i] = y0[i] + theta * (ydiff + th1 * (bspl + theta * (r4 + th1 * dd[i])));
+  }
 }
 
 // One DOP853 attempt: 11 new stages; the 5th- and 3rd-order error estimates

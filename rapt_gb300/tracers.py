@@ -35,7 +35,7 @@ def _config(eom=0, tableau=0):
     return dict(rtol=rtol, atol=atol, cyclotronresolution=p["cyclotronresolution"], gctimestep=p["GCtimestep"],
                 epss=p["epss"], epst=p["epst"], enforce_equatorial=int(bool(p["enforce equatorial"])),
                 gc_eom=eom, tableau=tableau, bounceresolution=p["bounceresolution"],
-                fieldlineresolution=p["fieldlineresolution"])
+                fieldlineresolution=p["fieldlineresolution"], dense_output=int(bool(p.get("dense output", False))))
 
 
 class _Pickle:
@@ -423,7 +423,10 @@ def _estimate_rows(kind, tracers, delta):
         dmin = min(dts)
         if np.isfinite(dmin):
             n = max(n, int(np.ceil(np.max(delta) / dmin)) + 4)
-    return min(n, 4096) if kind == N.KIND_ADAPTIVE else n
+    n = min(n, 4096) if kind == N.KIND_ADAPTIVE else n
+    if p.get("dense output", False) and kind != N.KIND_PARTICLE:
+        n = max(n, 18)  # a dense-output step may cover 17 output times
+    return n
 
 
 def _raise_if_left_grid(res):

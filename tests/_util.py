@@ -118,3 +118,15 @@ def synth_grid(times, static=True):
 def oracle_grid(O, g):
     """The oracle's copy of a facade Grid."""
     return O.grid_field(g._t, g._x, g._y, g._z, g._B, g._E, static=g.static)
+
+
+def within_envelope(err, env):
+    """Device-oracle differences against the oracle's own divergence under a
+    1e-15 perturbation of the start: the same distribution up to small factors
+    (one perturbed run is a noisy per-tracer estimate, so the tail is bounded as
+    a distribution, not tracer by tracer)."""
+    assert np.median(err) <= max(1e-12, 10 * np.median(env)), (np.median(err), np.median(env))
+    assert np.quantile(err, 0.9) <= max(1e-11, 10 * np.quantile(env, 0.9)), (np.quantile(err, 0.9),
+                                                                              np.quantile(env, 0.9))
+    assert err.max() <= max(1e-9, 10 * env.max()), (err.max(), env.max())
+    assert np.mean(err > np.maximum(1e-9, 100 * env)) <= 0.03

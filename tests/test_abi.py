@@ -38,7 +38,9 @@ def test_abi_version_and_defaults():
 
 def test_struct_layouts_match_header():
     # field order and sizes of rapt_config / rapt_host_state / rapt_stats / rapt_gc_device_state
-    assert C.sizeof(N.RaptConfig) == 8 * 6 + 4 * 4 + 8 * 2 + 4 * 2 + 8 + 4 * 2 + 4 + 4 + 8 + 4 + 4 + 8 + 8  # collect, pad, learned_scale, learned_every, per_tracer_launches, bounce/fieldline res
+    # ... collect, pad, learned_scale, learned_every, per_tracer_launches, bounce/fieldline res,
+    # dense_output + tail padding
+    assert C.sizeof(N.RaptConfig) == 8 * 6 + 4 * 4 + 8 * 2 + 4 * 2 + 8 + 4 * 2 + 4 + 4 + 8 + 4 + 4 + 8 + 8 + 8
     assert C.sizeof(N.RaptHostState) == 8 * 21
     assert C.sizeof(N.RaptStats) == 8 * 9
     assert C.sizeof(N.RaptGcDeviceState) == 8 * 18

@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from tests._util import oracle_grid, rel_state_error, synth_grid
+from tests._util import oracle_grid, rel_state_error, synth_grid, within_envelope
 from tests.golden import grid_data as GD
 
 pytestmark = pytest.mark.gpu
@@ -192,18 +192,6 @@ def _oracle_gc(oracle, of, pos, vg, pa, t0, delta, rtol, eps=0.0):
     return tr
 
 
-def _within_envelope(err, env):
-    """Device-oracle differences against the oracle's own divergence under a
-    1e-15 perturbation of the start: the same distribution up to small factors
-    (one perturbed run is a noisy per-tracer estimate, so the tail is bounded as
-    a distribution, not tracer by tracer)."""
-    assert np.median(err) <= max(1e-12, 10 * np.median(env)), (np.median(err), np.median(env))
-    assert np.quantile(err, 0.9) <= max(1e-11, 10 * np.quantile(env, 0.9)), (np.quantile(err, 0.9),
-                                                                              np.quantile(env, 0.9))
-    assert err.max() <= max(1e-9, 10 * env.max()), (err.max(), env.max())
-    assert np.mean(err > np.maximum(1e-9, 100 * env)) <= 0.03
-
-
 def test_grid_ensembles_match_oracle(oracle):
     """2048 protons and 2048 electron guiding centres in the five-snapshot field
     (static False) against the oracle, tracer by tracer. Linear interpolation
@@ -241,8 +229,8 @@ def test_grid_ensembles_match_oracle(oracle):
     assert ok.mean() > 0.9
     pos_err, mom_err = rel_state_error(h["s"][:, ok], tr["s"][ok], 6)
     env_pos, env_mom = rel_state_error(tp["s"][ok].T, tr["s"][ok], 6)
-    _within_envelope(pos_err, env_pos)
-    _within_envelope(mom_err, env_mom)
+    within_envelope(pos_err, env_pos)
+    within_envelope(mom_err, env_mom)
     # guiding centres from t0 = 0.5 s (the time-derivative stencil needs t - 1e-3 >= 0)
     pos = _ensemble(n, rng)
     vg = rng.uniform(1e7, 1e8, n)
@@ -260,8 +248,8 @@ def test_grid_ensembles_match_oracle(oracle):
     assert ok.mean() > 0.9
     pos_err, ppar_err = rel_state_error(h["s"][:, ok], tr["s"][ok], 4)
     env_pos, env_ppar = rel_state_error(tp["s"][ok].T, tr["s"][ok], 4)
-    _within_envelope(pos_err, env_pos)
-    _within_envelope(ppar_err, env_ppar)
+    within_envelope(pos_err, env_pos)
+    within_envelope(ppar_err, env_ppar)
     assert np.allclose(h["t_row"][ok], tr["t"][ok], rtol=1e-12, atol=0)
 
 
