@@ -54,12 +54,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1 << 20, help="tracers per GPU")
+    ap.add_argument("--bc-delta", type=float, default=2.0, help="bc_drift_65k: BounceCenter.advance(delta) per step")
     ap.add_argument("--cpu-sample", type=int, default=0, help="tracers in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="gc_doubledipole_1M",
                     choices=["gc_doubledipole_1M", "harris_adaptive_262k", "earthdipole_particles", "compressed_adaptive",
-                             "gc_grid_262k", "gc_dense_cadence"],
+                             "gc_grid_262k", "gc_dense_cadence", "bc_drift_65k"],
                     help="gc_doubledipole_1M: the headline metric; harris_adaptive_262k: the batching comparison; "
                          "earthdipole_particles (config 4) and compressed_adaptive (config 5): form comparisons "
                          "on --n tracers")
@@ -613,6 +614,95 @@ def run_dense_workload(args, rank, ws, dist):
     print(json.dumps(line), flush=True)
 
 
+def _bc_inputs(w, magB):
+    c = 299792458.0
+    gamma = 1.0 / np.sqrt(1.0 - (w["v"] / c) ** 2)
+    mu = gamma ** 2 * w["mass"] * (w["v"] * np.sin(np.deg2rad(w["eqpa"]))) ** 2 / (2 * magB)
+    st = np.column_stack([np.zeros(len(mu)), w["pos"], np.zeros(len(mu))])
+    cst = np.column_stack([w["v"], mu, w["mass"], w["charge"]])
+    return st, cst
+
+
+def bc_cpu_baseline(w, st, cst, delta, n_sample, threads):
+    """The oracle's BounceCenter.advance (same algorithm: converged integrals) on
+    a sample, one tracer per host thread."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    idx = np.linspace(0, len(cst) - 1, n_sample).astype(np.int64)
+    f = O.field("DoubleDipole")
+    p = w["params"]
+
+    def one(i):
+        cfg = O.config(rtol=p["rtol"], atol=p["atol"])
+        s = st[i].copy()
+        _, rows, cnt = O.bc_advance(f, cfg, s, cst[i, 0], cst[i, 1], cst[i, 2], cst[i, 3], delta, p["bctimestep"],
+                                    p["eyegradientstep"], quad=1)
+        return len(rows), int(cnt[0])
+
+    t = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:  # ctypes releases the GIL during each call
+        res = list(ex.map(one, idx))
+    dt = time.perf_counter() - t
+    return sum(r[1] for r in res) / dt, n_sample * delta / dt, dt
+
+
+def run_bc_workload(args, rank, ws, dist):
+    """Bounce centres (BounceCenter.advance): 65,536 protons in the DoubleDipole
+    field advanced 2 s per step; each right-hand side traces five field lines
+    (the half-bounce path and four second invariants for grad I). Simulated
+    tracer-seconds/s and right-hand sides/s, against the oracle on host cores."""
+    from rapt_gb300 import workloads as W, fields as F, _native as N
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx = N.Context(dev)
+    n = args.n if args.n != (1 << 20) else (1 << 16)
+    w = W.bc_drift(1 << 16, seed=rank)
+    if n < (1 << 16):  # an evenly spaced subset of the 65,536
+        w = W.subsample(w, np.arange(0, 1 << 16, (1 << 16) // n)[:n])
+    F.DoubleDipole().bind(ctx)
+    ctx.set_config(rtol=w["params"]["rtol"], atol=w["params"]["atol"])
+    magB = ctx.field_eval("magB", np.column_stack([np.zeros(n), w["pos"]]))[:, 0]
+    st0, cst = _bc_inputs(w, magB)
+    delta = args.bc_delta
+    p = w["params"]
+    steps, warmup = max(1, min(args.steps, 3)), min(args.warmup, 1)
+    st = st0.copy()
+    for _ in range(warmup):
+        st, rows, nr, status, cnt = ctx.bc_advance(st, cst, delta, p["bctimestep"], p["eyegradientstep"], 32)
+    clk = Clocks(dev) if rank == 0 else None
+    barrier(dist)
+    t0 = time.perf_counter()
+    rhs = acc = nrows = 0
+    for _ in range(steps):
+        st, rows, nr, status, cnt = ctx.bc_advance(st, cst, delta, p["bctimestep"], p["eyegradientstep"], 32)
+        rhs += int(cnt[:, 0].sum())
+        acc += int(cnt[:, 2].sum())
+        nrows += int(nr.sum())
+    barrier(dist)
+    wall = allmax(dist, time.perf_counter() - t0)
+    clocks = clk.stop() if clk else None
+    if rank != 0:
+        return
+    line = {"metric": "simulated bounce-centre seconds/s", "workload": "bc_drift_65k",
+            "value": allsum(dist, float(n * steps * delta)) / wall, "unit": "tracer-seconds/s", "n_gpus": ws,
+            "steps": steps, "warmup": warmup, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (seeded; protons L 4-7, 0.5-5 MeV, equatorial pitch angle 70-88 deg)",
+            "config": {"workload": "bc_drift_65k", "tracers_per_gpu": n, "field": "DoubleDipole",
+                       "step": "BounceCenter.advance(%g)" % delta, "bctimestep": p["bctimestep"],
+                       "eyegradientstep_re": 0.03, "timing": "host wall clock around rapt_bc_advance "
+                       "(copies and per-row launches included)"},
+            "rhs_per_s": allsum(dist, rhs) / wall, "accepted_per_s": allsum(dist, acc) / wall,
+            "field_line_traces_per_s": 5 * allsum(dist, rhs) / wall, "rows": nrows,
+            "status_counts": {int(k): int(v) for k, v in zip(*np.unique(status, return_counts=True))},
+            "clocks": clocks}
+    if not args.no_cpu_baseline:
+        n_s = args.cpu_sample or 256
+        v, ts, dt = bc_cpu_baseline(w, st0, cst, delta, n_s, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": ts, "unit": "tracer-seconds/s", "rhs_per_s": v, "cores": os.cpu_count(),
+                                "kind": "port", "sample": "%d of the %d bounce centres, %g s each (%.1f s)" % (
+                                    n_s, n, delta, dt)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, ws, dist = dist_init(args)
@@ -626,6 +716,8 @@ def main():
         run_grid_workload(args, rank, ws, dist)
     elif args.workload == "gc_dense_cadence":
         run_dense_workload(args, rank, ws, dist)
+    elif args.workload == "bc_drift_65k":
+        run_bc_workload(args, rank, ws, dist)
     else:
         run_ours(args, rank, ws, dist)
     if dist is not None:

@@ -229,6 +229,32 @@ int rapt_rhs_eval(void* ctx, int mode, int64_t n, const double* state, const dou
  * config's fieldlineresolution. */
 int rapt_gc_bounce_period(void* ctx, int64_t n, const double* state, double* out);
 
+/* --- BounceCenter (rapt/BounceCenter.py) and the second invariant ----------
+ * BounceCenter.advance(delta) (BounceCenter.py:214-252) for n bounce centres at
+ * once, one GPU thread each (field-line traces in a 64 KB scratch slot): the
+ * drift gamma m v^2 / (q S_b |B|^2) (grad I x B) with S_b = halfbouncepath
+ * and grad I = flutils.gradI (five field-line traces per right-hand side),
+ * rows every bctimestep x the bounce period at the start, SciPy-dopri5
+ * restarts per row (config rtol, atol, nsteps; fieldlineresolution).
+ *   state[n][5] in/out = (t, x, y, z, tcur): t, x, y, z = trajectory[-1]
+ *   cst[n][4] = (v, mu, mass, charge)
+ *   rows[n][max_rows][4] out = (t, x, y, z): the reference's rows, each stamped
+ *     with the time its interval began (np.arange(tcur, tcur + delta, dt));
+ *     nrows[n] out counts all rows (rows past max_rows are not stored)
+ *   status[n] out: RAPT_ST_*; counters[n][4] (NFCN, NSTEP, NACCPT, NREJCT) or NULL
+ * The field must be static (BounceCenter.py:95-97). The reference's
+ * flutils.eye raises NameError below 70 degrees equatorial pitch angle (its
+ * Simpson branch calls an undefined name); the device uses the spline branch
+ * at every pitch angle. */
+int rapt_bc_advance(void* ctx, int64_t n, double* state, const double* cst, double delta, double bctimestep,
+                    double eyegradientstep, double* rows, int32_t max_rows, int32_t* nrows, int32_t* status,
+                    int64_t* counters);
+/* Checks at tpos[n][4] with mirror fields Bm[n]: what 0 flutils.eye (out[n][3],
+ * first value), 1 flutils.gradI, 2 the bounce-averaged drift velocity (needs
+ * cst[n][4] as above). NaN where a trace overflows or the reference raises. */
+int rapt_bc_eval(void* ctx, int what, int64_t n, const double* tpos, const double* Bm, double eyegradientstep,
+                 const double* cst, double* out);
+
 /* --- allocation-free guiding-centre advance ------------------------------- */
 /* No counterpart in the reference: RAPT has no device code and no notion of
  * memory ownership. This entry point is for callers that cannot call

@@ -99,6 +99,9 @@ bool rkf_segment(const orc_field* f, double time, double sign, const double* x0,
 void trace_sB(const orc_field* f, const double* tpos, double Bm, double flres, std::vector<double>& s,
               std::vector<double>& B) {
   const double ds = 1.0 / orc_curvature(f, tpos) / flres;  // fieldline.py:31-35
+  s.clear();
+  B.clear();
+  if (!(ds > 0) || !std::isfinite(ds)) return;  // a non-finite start (the device's trace gives up too)
   const double init[4] = {0.0, tpos[1], tpos[2], tpos[3]};
   std::vector<double> fw(init, init + 4), bw(init, init + 4);
   for (int dir = 0; dir < 2; ++dir) {
@@ -650,6 +653,35 @@ void gauss_legendre8(double* x, double* w) {
 // s = c + h sin(theta) removes the inverse-square-root singularities at the
 // mirror points, and an 8-point Gauss-Legendre rule runs on every panel between
 // the images of the spline's knots (each panel a smooth polynomial piece).
+// The same rule for the second invariant's integrand sqrt(1 - B(s)/Bm), which
+// the substitution leaves smooth as well.
+double eye_integral_converged(const Spline2& sp, double sm1, double sm2, double Bm) {
+  double gx[8], gw[8];
+  gauss_legendre8(gx, gw);
+  const double c = 0.5 * (sm1 + sm2), h = 0.5 * (sm2 - sm1);
+  double sum = 0.0, ea = -kPiF / 2;
+  for (int j = 3; j <= sp.n; ++j) {
+    double eb;
+    if (j < sp.n) {
+      const double tj = sp.t[j];
+      if (!(tj > sm1 && tj < sm2)) continue;
+      eb = std::asin((tj - c) / h);
+    } else {
+      eb = kPiF / 2;
+    }
+    const double mid = 0.5 * (ea + eb), half = 0.5 * (eb - ea);
+    double ps = 0.0;
+    for (int k = 0; k < 8; ++k) {
+      const double th = mid + half * gx[k];
+      const double arg = 1.0 - sp(c + h * std::sin(th)) / Bm;
+      if (arg > 0.0) ps += gw[k] * (h * std::cos(th) * std::sqrt(arg));
+    }
+    sum += half * ps;
+    ea = eb;
+  }
+  return sum;
+}
+
 double bounce_integral_converged(const Spline2& sp, double sm1, double sm2, double Bm) {
   double gx[8], gw[8];
   gauss_legendre8(gx, gw);
@@ -746,6 +778,73 @@ double orc_halfbouncepath(const orc_field* f, const double* tpos, double Bm, dou
   if (quad == 1) return bounce_integral_converged(sp, sm1, sm2, Bm);
   int ier = 0;
   return qags([&](double x) { return 1 / std::sqrt(1 - sp(x) / Bm); }, sm1, sm2, 1.49e-8, 1e-4, 50, ier);
+}
+
+double orc_eye(const orc_field* f, const double* tpos, double Bm, double flres, int quad) {
+  // flutils.eye, rapt/flutils.py:65-151 (usedipole False). quad 0: as the
+  // reference -- equatorial pitch angles below 70 degrees take its Simpson
+  // branch, which calls the undefined name simps (flutils.py:18, :130) and
+  // raises NameError: NaN here; 70 and above: quadratic spline, brentq mirror
+  // points, QAGS at epsrel 1e-4. quad 1: the spline branch at every pitch angle,
+  // integrated to convergence (the device's method).
+  std::vector<double> s, b;
+  trace_sB(f, tpos, Bm, flres, s, b);
+  const int n0 = (int)b.size();
+  if (n0 == 0) return NAN;
+  double Bmin = b[0];
+  for (int i = 1; i < n0; ++i) Bmin = std::min(Bmin, b[i]);
+  if (Bmin > Bm) return 0.0;
+  if (std::fabs(Bmin - Bm) / Bm < 1e-12) return 0.0;  // equatorial particle
+  int first = -1, last = -1;
+  for (int i = 0; i < n0; ++i)
+    if (b[i] < Bm) {
+      if (first < 0) first = i;
+      last = i;
+    }
+  // np.delete of range(0, first - 1) and range(last + 2, n): keep first-1 .. last+1
+  const int lo = std::max(first - 1, 0), hi = std::min(last + 1, n0 - 1);
+  std::vector<double> ss(s.begin() + lo, s.begin() + hi + 1), bb(b.begin() + lo, b.begin() + hi + 1);
+  const int n = (int)bb.size();
+  if (!(n >= 3 && bb[0] > Bm && bb[1] < Bm && bb[n - 2] < Bm && bb[n - 1] > Bm)) return NAN;  // AssertionError
+  const double eqpa = std::asin(std::sqrt(Bmin / Bm)) * 180 / kPiF;
+  if (quad == 0 && eqpa < 70) return NAN;  // NameError in the reference
+  Spline2 sp;
+  sp.build(ss.data(), bb.data(), n);
+  auto g = [&](double x) { return sp(x) - Bm; };
+  const double xtol = 2e-12, rtol = 4 * DBL_EPSILON;
+  const double sm1 = brentq(g, ss[0], ss[1], xtol, rtol, 100);
+  const double sm2 = sp(ss[n - 2]) == Bm ? ss[n - 2] : brentq(g, ss[n - 2], ss[n - 1], xtol, rtol, 100);
+  if (quad == 1) return eye_integral_converged(sp, sm1, sm2, Bm);
+  int ier = 0;
+  return qags([&](double x) { return std::sqrt(1 - sp(x) / Bm); }, sm1, sm2, 1.49e-8, 1e-4, 50, ier);
+}
+
+void orc_gradI(const orc_field* f, const double* tpos, double Bm, double d, double flres, int quad, double* out) {
+  // flutils.gradI, rapt/flutils.py:153-229 (usedipole False): central differences
+  // of I over d in two directions perpendicular to b, one-sided where an end
+  // has I = 0
+  const double x = tpos[1], y = tpos[2];
+  const double sc = std::max(std::fabs(x), std::fabs(y));
+  double r[3] = {x / sc, y / sc, 0.0 / sc};
+  double b[3];
+  orc_unitb(f, tpos, b);
+  const double rb = r[0] * b[0] + r[1] * b[1] + r[2] * b[2];
+  for (int i = 0; i < 3; ++i) r[i] = r[i] - rb * b[i];
+  const double rn = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  for (int i = 0; i < 3; ++i) r[i] = r[i] / rn;
+  const double v2[3] = {b[1] * r[2] - b[2] * r[1], b[2] * r[0] - b[0] * r[2], b[0] * r[1] - b[1] * r[0]};
+  const double* dirs[2] = {r, v2};
+  double dI[2];
+  for (int k = 0; k < 2; ++k) {
+    const double* v = dirs[k];
+    double tp[4] = {tpos[0], tpos[1] + d * v[0], tpos[2] + d * v[1], tpos[3] + d * v[2]};
+    double tm[4] = {tpos[0], tpos[1] - d * v[0], tpos[2] - d * v[1], tpos[3] - d * v[2]};
+    const double I1 = orc_eye(f, tp, Bm, flres, quad), I2 = orc_eye(f, tm, Bm, flres, quad);
+    if (I1 == 0) dI[k] = (orc_eye(f, tpos, Bm, flres, quad) - I2) / d;
+    else if (I2 == 0) dI[k] = (I1 - orc_eye(f, tpos, Bm, flres, quad)) / d;
+    else dI[k] = (I1 - I2) / (2 * d);
+  }
+  for (int i = 0; i < 3; ++i) out[i] = dI[0] * r[i] + dI[1] * v2[i];
 }
 
 double orc_gc_bounceperiod(const orc_field* f, const orc_tracer* g, double flres, int quad) {

@@ -110,6 +110,12 @@ def lib():
             "orc_halfbouncepath": (_d, [F, _dp, _d, _d, C.c_int, _P(C.c_int)]),
             "orc_fieldline_sB": (C.c_int, [F, _dp, _d, _d, _dp, _dp, C.c_int]),
             "orc_qags_test": (_d, [C.c_int, _d, _d, _d, _d, C.c_int, _P(C.c_int)]),
+            "orc_eye": (_d, [F, _dp, _d, _d, C.c_int]),
+            "orc_gradI": (None, [F, _dp, _d, _d, _d, C.c_int, _dp]),
+            "orc_bc_mu": (_d, [F, _dp, _d, _d, _d, _d]),
+            "orc_bc_rhs": (None, [F, _dp, _d, _d, _d, _d, _d, _d, C.c_int, _dp]),
+            "orc_bc_advance": (C.c_int, [F, Cf, _dp, _d, _d, _d, _d, _d, _d, _d, C.c_int, _dp, C.c_int,
+                                         _P(C.c_int), _P(C.c_int64)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -287,3 +293,44 @@ def qags_test(which, a, b, epsabs=1.49e-8, epsrel=1.49e-8, limit=50):
     ier = C.c_int(0)
     r = lib().orc_qags_test(int(which), float(a), float(b), float(epsabs), float(epsrel), int(limit), C.byref(ier))
     return r, ier.value
+
+
+def eye(f, tpos, Bm, flres=50.0, quad=0):
+    """flutils.eye: NaN where the reference raises."""
+    tp, ptp = _vec(tpos, 4)
+    return lib().orc_eye(C.byref(f), ptp, float(Bm), float(flres), int(quad))
+
+
+def gradI(f, tpos, Bm, d, flres=50.0, quad=0):
+    tp, ptp = _vec(tpos, 4)
+    out = np.zeros(3)
+    lib().orc_gradI(C.byref(f), ptp, float(Bm), float(d), float(flres), int(quad), out.ctypes.data_as(_dp))
+    return out
+
+
+def bc_mu(f, pos, v, pa, t0, mass):
+    p, pp = _vec(pos, 3)
+    return lib().orc_bc_mu(C.byref(f), pp, float(v), float(pa), float(t0), float(mass))
+
+
+def bc_rhs(f, tpos, mass, charge, v, Bm, d, flres=50.0, quad=0):
+    tp, ptp = _vec(tpos, 4)
+    out = np.zeros(3)
+    lib().orc_bc_rhs(C.byref(f), ptp, float(mass), float(charge), float(v), float(Bm), float(d), float(flres),
+                     int(quad), out.ctypes.data_as(_dp))
+    return out
+
+
+def bc_advance(f, cfg, state, v, mu, mass, charge, delta, bctimestep, d, quad=0, max_rows=10000):
+    """BounceCenter.advance; state = (t, x, y, z, tcur) updated in place.
+    Returns (status, rows[n, 4], counters[4])."""
+    st = np.ascontiguousarray(state, dtype=np.float64)
+    assert st.size == 5
+    rows = np.zeros((max_rows, 7))
+    n = C.c_int(0)
+    cnt = np.zeros(4, np.int64)
+    status = lib().orc_bc_advance(C.byref(f), C.byref(cfg), st.ctypes.data_as(_dp), float(v), float(mu),
+                                  float(mass), float(charge), float(delta), float(bctimestep), float(d), int(quad),
+                                  rows.ctypes.data_as(_dp), max_rows, C.byref(n), cnt.ctypes.data_as(_P(C.c_int64)))
+    state[:] = st
+    return status, rows[:n.value, :4].copy(), cnt

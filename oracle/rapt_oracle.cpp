@@ -1197,6 +1197,65 @@ int orc_gc_advance(const orc_field* f, const orc_config* c, orc_tracer* g, doubl
   return 0;
 }
 
+// ---------------------------------------------------------------- BounceCenter
+double orc_bc_mu(const orc_field* f, const double* pos, double v, double pa, double t0, double mass) {
+  // BounceCenter.__init__, rapt/BounceCenter.py:100-104: the parallel speed is
+  // v cos(pa) with pa in degrees handed to np.cos as radians (kept)
+  return magnetic_moment(f, t0, pos, v * std::cos(pa), v, mass);
+}
+
+void orc_bc_rhs(const orc_field* f, const double* tpos, double mass, double charge, double v, double Bm, double d,
+                double flres, int quad, double* o) {
+  // BounceCenter.advance deriv (BounceCenter.py:236-245), the non-equatorial
+  // branch: gamma m v^2 / (q S_b B^2) (grad I x B)
+  const double gamma = 1.0 / std::sqrt(1 - (v / kC) * (v / kC));
+  double B[3], gI[3];
+  orc_B(f, tpos, B);
+  const double magBsq = dot3(B, B);
+  const double Sb = orc_halfbouncepath(f, tpos, Bm, flres, quad, nullptr);
+  orc_gradI(f, tpos, Bm, d, flres, quad, gI);
+  const double k = gamma * mass * v * v / (charge * Sb * magBsq);
+  o[0] = k * (gI[1] * B[2] - gI[2] * B[1]);
+  o[1] = k * (gI[2] * B[0] - gI[0] * B[2]);
+  o[2] = k * (gI[0] * B[1] - gI[1] * B[0]);
+}
+
+int orc_bc_advance(const orc_field* f, const orc_config* c, double* state, double v, double mu, double mass,
+                   double charge, double delta, double bctimestep, double d, int quad, double* rows, int max_rows,
+                   int* nrows, int64_t* counters4) {
+  // BounceCenter.advance, rapt/BounceCenter.py:214-252: cadence BCtimestep x the
+  // bounce period at the start; rows stamped with np.arange(tcur, tcur + delta,
+  // dt), i.e. each row carries the time its interval began (kept); one SciPy
+  // dopri5 restart per row
+  const double gamma = 1.0 / std::sqrt(1 - (v / kC) * (v / kC));
+  const double Bm = mass * (gamma * gamma) * (v * v) / (2 * mu);
+  double tpos[4] = {state[0], state[1], state[2], state[3]};
+  const double bp = (2 / v) * orc_halfbouncepath(f, tpos, Bm, c->flres, quad, nullptr);
+  const double dt = bctimestep * bp;
+  if (!(dt > 0) || !std::isfinite(dt)) return ORC_ST_FIELDLINE;
+  const double tcur = state[4];
+  const int64_t K = (int64_t)std::ceil(((tcur + delta) - tcur) / dt);
+  const double dstep = (tcur + dt) - tcur;
+  auto rhs = [&](double t, const double* Y, double* o) {
+    const double tp[4] = {t, Y[0], Y[1], Y[2]};
+    orc_bc_rhs(f, tp, mass, charge, v, Bm, d, c->flres, quad, o);
+  };
+  double rt = state[0], y[3] = {state[1], state[2], state[3]};
+  int status = ORC_ST_OK;
+  for (int64_t k = 0; k < K; ++k) {
+    const double tk = k == 0 ? tcur : (k == 1 ? tcur + dt : tcur + (double)k * dstep);
+    Counters cnt;
+    const int idid = dopri5(rhs, 3, rt, y, rt + dt, c->rtol, c->atol, c->nsteps, cnt);
+    counters4[0] += cnt.nfcn; counters4[1] += cnt.nstep; counters4[2] += cnt.naccpt; counters4[3] += cnt.nrejct;
+    if (idid < 0) status = idid == -2 ? ORC_ST_MAXSTEPS : ORC_ST_HMIN;
+    if (!finite_n(y, 3)) status = ORC_ST_NONFINITE;
+    put_row(rows, max_rows, nrows, tk, y, 3);
+    state[0] = tk; state[1] = y[0]; state[2] = y[1]; state[3] = y[2]; state[4] = tk;
+    if (status != ORC_ST_OK) break;
+  }
+  return status;
+}
+
 int orc_adaptive_init(const orc_field* f, const orc_config* c, const double* pos, const double* vel,
                       double t0, double mass, double charge, orc_tracer* out) {
   // Adaptive.__init__, rapt/Adaptive.py:70-104

@@ -138,6 +138,20 @@ int orc_gc_advance(const orc_field* f, const orc_config* c, orc_tracer* g, doubl
  * and composite Gauss-Legendre, the device's method). */
 double orc_gc_bounceperiod(const orc_field* f, const orc_tracer* g, double flres, int quad);
 double orc_halfbouncepath(const orc_field* f, const double* tpos, double Bm, double flres, int quad, int* npts);
+/* flutils.eye and flutils.gradI (second invariant and its gradient), quad as above;
+ * eye is NaN where the reference raises (its Simpson branch below 70 degrees
+ * equatorial pitch angle calls an undefined name; failed trim assertion). */
+double orc_eye(const orc_field* f, const double* tpos, double Bm, double flres, int quad);
+void orc_gradI(const orc_field* f, const double* tpos, double Bm, double d, double flres, int quad, double* out3);
+/* BounceCenter (rapt/BounceCenter.py): the constructor's magnetic moment, the
+ * bounce-averaged drift velocity and advance(delta). state[5] = (t, x, y, z,
+ * tcur) in/out; rows[max_rows][4]. Returns a status. */
+double orc_bc_mu(const orc_field* f, const double* pos, double v, double pa, double t0, double mass);
+void orc_bc_rhs(const orc_field* f, const double* tpos, double mass, double charge, double v, double Bm, double d,
+                double flres, int quad, double* out3);
+int orc_bc_advance(const orc_field* f, const orc_config* c, double* state, double v, double mu, double mass,
+                   double charge, double delta, double bctimestep, double d, int quad, double* rows, int max_rows,
+                   int* nrows, int64_t* counters4);
 int orc_fieldline_sB(const orc_field* f, const double* tpos, double Bm, double flres, double* s, double* B,
                      int cap);
 double orc_qags_test(int which, double a, double b, double epsabs, double epsrel, int limit, int* ier);

@@ -66,6 +66,8 @@ SIGNATURES = {
     "rapt_field_set": (C.c_int, [_VP, C.c_int, _DP, C.c_int]),
     "rapt_field_set_steps": (C.c_int, [_VP, _D, _D]),
     "rapt_field_set_static": (C.c_int, [_VP, C.c_int]),
+    "rapt_bc_advance": (C.c_int, [_VP, _I64, _VP, _VP, _D, _D, _D, _VP, C.c_int32, _VP, _VP, _VP]),
+    "rapt_bc_eval": (C.c_int, [_VP, C.c_int, _I64, _VP, _VP, _D, _VP, _VP]),
     "rapt_grid_set": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, _VP, C.c_int32, _VP, C.c_int32, _VP, _VP, _VP]),
     "rapt_config_default": (None, [C.POINTER(RaptConfig)]),
     "rapt_config_set": (C.c_int, [_VP, C.POINTER(RaptConfig)]),
@@ -193,6 +195,32 @@ class Context:
                 raise ValueError("E must have the shape of B")
         self.check(self.L.rapt_grid_set(self.h, nt, ptr(a[0]), nx, ptr(a[1]), ny, ptr(a[2]), nz, ptr(a[3]),
                                         ptr(B), ptr(E) if E is not None else None), "rapt_grid_set")
+
+    def bc_advance(self, state, cst, delta, bctimestep, eyegradientstep, max_rows):
+        """BounceCenter.advance for n bounce centres: state[n][5] (t, x, y, z, tcur)
+        updated in place; returns (rows[n, max_rows, 4], nrows, status, counters)."""
+        state = np.ascontiguousarray(state, dtype=np.float64)
+        cst = np.ascontiguousarray(cst, dtype=np.float64)
+        n = state.shape[0]
+        rows = np.zeros((n, max_rows, 4))
+        nrows = np.zeros(n, np.int32)
+        status = np.zeros(n, np.int32)
+        cnt = np.zeros((n, 4), np.int64)
+        self.check(self.L.rapt_bc_advance(self.h, n, ptr(state), ptr(cst), float(delta), float(bctimestep),
+                                          float(eyegradientstep), ptr(rows), int(max_rows), ptr(nrows), ptr(status),
+                                          ptr(cnt)), "rapt_bc_advance")
+        return state, rows, nrows, status, cnt
+
+    def bc_eval(self, what, tpos, Bm, eyegradientstep, cst=None):
+        tpos = np.ascontiguousarray(np.atleast_2d(tpos), dtype=np.float64)
+        n = tpos.shape[0]
+        Bm = np.ascontiguousarray(np.broadcast_to(np.asarray(Bm, float), (n,)))
+        c = None if cst is None else np.ascontiguousarray(np.broadcast_to(np.asarray(cst, float), (n, 4)))
+        out = np.zeros((n, 3))
+        what = {"eye": 0, "gradI": 1, "drift": 2}.get(what, what)
+        self.check(self.L.rapt_bc_eval(self.h, int(what), n, ptr(tpos), ptr(Bm), float(eyegradientstep), ptr(c),
+                                       ptr(out)), "rapt_bc_eval")
+        return out
 
     def set_config(self, **kw):
         cfg = RaptConfig()

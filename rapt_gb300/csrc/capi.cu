@@ -4,11 +4,13 @@
 // of the ensemble, and a small scratch block (work-queue heads and counters of
 // the persistent kernels). rapt_advance() runs rounds of one launch per mode
 // until no tracer is left pending (Adaptive alternates modes across rounds).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "launch.h"
 
@@ -1030,6 +1032,119 @@ int rapt_gc_bounce_period(void* ctx, int64_t n, const double* state, double* out
                                           stride, kFieldlineCap, c->stream));
   CK(cudaMemcpyAsync(out, d_out, N * 8, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  return RAPT_OK;
+}
+
+// Per-thread field-line scratch for n concurrent traces (kFieldlineCap points per direction).
+static int ensure_fl_scratch(Ctx* c, size_t n) {
+  const size_t need = n * (size_t)(8LL * kFieldlineCap) * sizeof(double);
+  if (c->fl_bytes >= need) return RAPT_OK;
+  cudaFree(c->fl_scratch);
+  c->fl_scratch = nullptr;
+  c->fl_bytes = 0;
+  if (cudaMalloc(&c->fl_scratch, need) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, RAPT_ERR_NOMEM, "cudaMalloc(%zu bytes) for field-line traces failed", need);
+  }
+  c->fl_bytes = need;
+  return RAPT_OK;
+}
+
+// tracers per BounceCenter pass: their trace scratch (64 KB each, one slot per
+// thread) is 512 MiB, so that the passes' scratch traffic stays mostly in L2
+constexpr int64_t kBcChunk = 8192;
+
+int rapt_bc_advance(void* ctx, int64_t n, double* state, const double* cst, double delta, double bctimestep,
+                    double eyegradientstep, double* rows, int32_t max_rows, int32_t* nrows, int32_t* status,
+                    int64_t* counters) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || n < 0 || (n > 0 && (!state || !cst || !nrows || !status)) || max_rows < 0 || (max_rows > 0 && !rows))
+    return RAPT_ERR_INVALID;
+  if (!c->field_set) return fail(c, RAPT_ERR_STATE, "no field set");
+  if (!c->field.is_static)
+    return fail(c, RAPT_ERR_UNSUPPORTED, "BounceCenter works with static fields only (BounceCenter.py:95-97)");
+  if (!(bctimestep > 0) || !(eyegradientstep > 0) || !std::isfinite(delta))
+    return fail(c, RAPT_ERR_INVALID, "bad BCtimestep, eyegradientstep or delta");
+  if (n == 0) return RAPT_OK;
+  CK(cudaSetDevice(c->device));
+  const long long stride = 8LL * kFieldlineCap;
+  const int64_t chunk = std::min<int64_t>(n, kBcChunk);
+  int rc = ensure_fl_scratch(c, (size_t)chunk);
+  if (rc) return rc;
+  KParams P = make_params(c, RAPT_KIND_GC);
+  const ModelTable& T = c->tab[c->field.model];
+  // device block per pass: st 5 | cst 4 | plan 4 | counters 4 (int64) | status, nrows (int32) | rows
+  const size_t C = (size_t)chunk, R = (size_t)max_rows;
+  rc = ensure_tmp(c, C * (17 * 8 + 2 * 4) + C * R * 4 * 8);
+  if (rc) return rc;
+  char* base = static_cast<char*>(c->tmp);
+  double* d_st = reinterpret_cast<double*>(base);
+  double* d_cst = d_st + 5 * C;
+  double* d_plan = d_cst + 4 * C;
+  int64_t* d_cnt = reinterpret_cast<int64_t*>(d_plan + 4 * C);
+  int32_t* d_status = reinterpret_cast<int32_t*>(d_cnt + 4 * C);
+  int32_t* d_nrows = d_status + C;
+  double* d_rows = reinterpret_cast<double*>(d_nrows + C);  // 17C doubles + 2C int32: 8-byte aligned
+  std::vector<double> plan;
+  for (int64_t k0 = 0; k0 < n; k0 += chunk) {
+    const int64_t m = std::min(chunk, n - k0);
+    const size_t M = (size_t)m;
+    CK(cudaMemcpyAsync(d_st, state + 5 * k0, M * 5 * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d_cst, cst + 4 * k0, M * 4 * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(d_cnt, 0, M * 4 * 8, c->stream));
+    CK(cudaMemsetAsync(d_nrows, 0, M * 4, c->stream));
+    CK(T.bc_start(c->field, c->cfg.fieldlineresolution, m, d_st, d_cst, delta, bctimestep, d_plan, d_status,
+                  c->fl_scratch, stride, kFieldlineCap, c->stream));
+    plan.resize(M * 4);
+    CK(cudaMemcpyAsync(plan.data(), d_plan, M * 4 * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    double kmax = 0.0;
+    for (size_t i = 0; i < M; ++i) kmax = std::max(kmax, plan[4 * i + 2]);
+    if (kmax > 1e7) return fail(c, RAPT_ERR_INVALID, "more than 1e7 rows per BounceCenter (delta / dt)");
+    for (int64_t j = 0; j < (int64_t)kmax; ++j)
+      CK(T.bc_interval(c->field, P, m, d_st, d_cst, d_plan, eyegradientstep, j, d_rows, max_rows, d_nrows, d_status,
+                       d_cnt, c->fl_scratch, stride, kFieldlineCap, c->stream));
+    CK(cudaMemcpyAsync(state + 5 * k0, d_st, M * 5 * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(status + k0, d_status, M * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(nrows + k0, d_nrows, M * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (max_rows > 0)
+      CK(cudaMemcpyAsync(rows + (size_t)k0 * R * 4, d_rows, M * R * 4 * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (counters) CK(cudaMemcpyAsync(counters + 4 * k0, d_cnt, M * 4 * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return RAPT_OK;
+}
+
+int rapt_bc_eval(void* ctx, int what, int64_t n, const double* tpos, const double* Bm, double eyegradientstep,
+                 const double* cst, double* out) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || what < 0 || what > 2 || n < 0 || (n > 0 && (!tpos || !Bm || !out || (what == 2 && !cst))))
+    return RAPT_ERR_INVALID;
+  if (!c->field_set) return fail(c, RAPT_ERR_STATE, "no field set");
+  if (n == 0) return RAPT_OK;
+  CK(cudaSetDevice(c->device));
+  const long long stride = 8LL * kFieldlineCap;
+  const int64_t chunk = std::min<int64_t>(n, kBcChunk);
+  int rc = ensure_fl_scratch(c, (size_t)chunk);
+  if (rc) return rc;
+  const size_t C = (size_t)chunk;
+  rc = ensure_tmp(c, C * 12 * 8);
+  if (rc) return rc;
+  double* d_tp = static_cast<double*>(c->tmp);
+  double* d_bm = d_tp + 4 * C;
+  double* d_cst = d_bm + C;
+  double* d_out = d_cst + 4 * C;
+  for (int64_t k0 = 0; k0 < n; k0 += chunk) {
+    const int64_t m = std::min(chunk, n - k0);
+    const size_t M = (size_t)m;
+    CK(cudaMemcpyAsync(d_tp, tpos + 4 * k0, M * 4 * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d_bm, Bm + k0, M * 8, cudaMemcpyHostToDevice, c->stream));
+    if (what == 2) CK(cudaMemcpyAsync(d_cst, cst + 4 * k0, M * 4 * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(c->tab[c->field.model].bc_eval(c->field, c->cfg.fieldlineresolution, what, m, d_tp, d_bm, eyegradientstep,
+                                      d_cst, d_out, c->fl_scratch, stride, kFieldlineCap, c->stream));
+    CK(cudaMemcpyAsync(out + 3 * k0, d_out, M * 3 * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
   return RAPT_OK;
 }
 

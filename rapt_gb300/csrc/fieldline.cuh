@@ -292,6 +292,9 @@ __device__ __forceinline__ void gauss_legendre8(double* x, double* w) {
   }
 }
 
+// INV: integrand 1/sqrt(1 - B/Bm) (half-bounce path); otherwise sqrt(1 - B/Bm)
+// (the second invariant I), which the substitution leaves smooth as well.
+template <bool INV = true>
 static __device__ __noinline__ double fl_bounce_integral(const DSpline2& sp, double sm1, double sm2, double Bm) {
   double gx[8], gw[8];
   gauss_legendre8(gx, gw);
@@ -312,7 +315,7 @@ static __device__ __noinline__ double fl_bounce_integral(const DSpline2& sp, dou
     for (int k = 0; k < 8; ++k) {
       const double th = da(mid, dm(half, gx[k]));
       const double arg = da(1.0, -(sp(da(c, dm(h, sin(th)))) / Bm));
-      if (arg > 0.0) ps = da(ps, dm(gw[k], dm(h, cos(th)) / sqrt(arg)));
+      if (arg > 0.0) ps = da(ps, dm(gw[k], INV ? dm(h, cos(th)) / sqrt(arg) : dm(dm(h, cos(th)), sqrt(arg))));
     }
     sum = da(sum, dm(half, ps));
     ea = eb;
@@ -324,15 +327,16 @@ static __device__ __noinline__ double fl_bounce_integral(const DSpline2& sp, dou
 // flutils.halfbouncepath (flutils.py:254-316) at position X, time t, mirror
 // field Bm. scratch: 4 * (2 * cap) doubles. Returns NaN where the trace
 // overflows the buffer or the result is not finite.
+// Fieldline(tpos, field, Bmax=Bm).trace() (fieldline.py:37-105) through X,
+// both directions joined in S, Bs [first, first + n0); false where the trace
+// overflows the buffer or the step is not finite.
 template <int M>
-__device__ __noinline__ double fl_halfbouncepath(const FieldP& f, double t, const double* X, double Bm,
-                                                 double flres, double* scratch, int cap) {
+__device__ bool fl_trace(const FieldP& f, double t, const double* X, double Bm, double flres, double* scratch,
+                         int cap, int& first, int& n0) {
   double* S = scratch;                 // [2 cap] arc length of the joined curve
-  double* Bs = scratch + 2 * cap;      // [2 cap] |B|, then the spline coefficients
-  double* di = scratch + 4 * cap;      // [2 cap]
-  double* up = scratch + 6 * cap;      // [2 cap]
+  double* Bs = scratch + 2 * cap;      // [2 cap] |B|
   const double ds = 1.0 / fl_curvature<M>(f, t, X) / flres;  // fieldline.py:31-35
-  if (!(ds > 0) || !isfinite(ds)) return nan("");
+  if (!(ds > 0) || !isfinite(ds)) return false;
   const int c0 = cap;  // slot of the start point
   S[c0] = 0.0;
   Bs[c0] = fl_magB<M>(f, t, X[0], X[1], X[2]);
@@ -353,9 +357,22 @@ __device__ __noinline__ double fl_halfbouncepath(const FieldP& f, double t, cons
       }
       if (Bs[idx] > Bm) break;
     }
-    if (overflow) return nan("");
+    if (overflow) return false;
   }
-  const int first = ibw, n0 = ifw - ibw + 1;  // joined curve: slots ibw .. ifw
+  first = ibw;
+  n0 = ifw - ibw + 1;  // joined curve: slots ibw .. ifw
+  return true;
+}
+
+template <int M>
+__device__ __noinline__ double fl_halfbouncepath(const FieldP& f, double t, const double* X, double Bm,
+                                                 double flres, double* scratch, int cap) {
+  double* S = scratch;                 // [2 cap] arc length of the joined curve
+  double* Bs = scratch + 2 * cap;      // [2 cap] |B|, then the spline coefficients
+  double* di = scratch + 4 * cap;      // [2 cap]
+  double* up = scratch + 6 * cap;      // [2 cap]
+  int first, n0;
+  if (!fl_trace<M>(f, t, X, Bm, flres, scratch, cap, first, n0)) return nan("");
   int fin = -1, lin = -1;
   for (int i = 0; i < n0; ++i)
     if (Bs[first + i] <= Bm) {
@@ -381,6 +398,76 @@ __device__ __noinline__ double fl_halfbouncepath(const FieldP& f, double t, cons
   const double sm1 = fl_brentq(g, s[0], s[1]);
   const double sm2 = fl_brentq(g, s[n - 2], s[n - 1]);
   return fl_bounce_integral(sp, sm1, sm2, Bm);
+}
+
+// flutils.eye (flutils.py:65-151), the second invariant I at X for mirror field
+// Bm, over the same trace: 0 where the line's minimum |B| exceeds Bm or equals
+// it (equatorial); the points with B < Bm plus one beyond each end; the
+// quadratic spline, brentq mirror points and the integral of sqrt(1 - B/Bm)
+// to convergence. The reference takes this spline branch at equatorial pitch
+// angles of 70 degrees and above; below, its Simpson branch calls an undefined
+// name and raises, and here the spline branch serves every pitch angle. NaN
+// where the trace overflows or the trimmed line fails the reference's assert.
+template <int M>
+__device__ __noinline__ double fl_eye(const FieldP& f, double t, const double* X, double Bm, double flres,
+                                     double* scratch, int cap) {
+  double* S = scratch;
+  double* Bs = scratch + 2 * cap;
+  double* di = scratch + 4 * cap;
+  double* up = scratch + 6 * cap;
+  int first, n0;
+  if (!fl_trace<M>(f, t, X, Bm, flres, scratch, cap, first, n0) || n0 < 1) return nan("");
+  double Bmin = Bs[first];
+  for (int i = 1; i < n0; ++i) Bmin = fmin(Bmin, Bs[first + i]);
+  if (Bmin > Bm) return 0.0;
+  if (fabs(Bmin - Bm) / Bm < 1e-12) return 0.0;
+  int fin = -1, lin = -1;
+  for (int i = 0; i < n0; ++i)
+    if (Bs[first + i] < Bm) {
+      if (fin < 0) fin = i;
+      lin = i;
+    }
+  const int lo = fin - 1 < 0 ? 0 : fin - 1, hi = lin + 1 > n0 - 1 ? n0 - 1 : lin + 1;
+  const int n = hi - lo + 1;
+  const double* s = S + first + lo;
+  double* b = Bs + first + lo;
+  if (!(n >= 3 && b[0] > Bm && b[1] < Bm && b[n - 2] < Bm && b[n - 1] > Bm)) return nan("");
+  spline2_solve(s, b, di, up, n);
+  const DSpline2 sp{s, b, n};
+  const MirrorFn g{sp, Bm};
+  const double sm1 = fl_brentq(g, s[0], s[1]);
+  const double sm2 = sp(s[n - 2]) == Bm ? s[n - 2] : fl_brentq(g, s[n - 2], s[n - 1]);
+  return fl_bounce_integral<false>(sp, sm1, sm2, Bm);
+}
+
+// flutils.gradI (flutils.py:153-229): central differences of I over d in the
+// two directions perpendicular to b built from (x, y, 0); one-sided where one
+// end has I = 0.
+template <int M>
+__device__ void fl_gradI(const FieldP& f, double t, const double* X, double Bm, double d, double flres,
+                         double* scratch, int cap, double* out) {
+  const double sc = fmax(fabs(X[0]), fabs(X[1]));
+  double r[3] = {X[0] / sc, X[1] / sc, 0.0 / sc};
+  double b[3], mag;
+  unit_and_mag<M>(f, t, X[0], X[1], X[2], b, mag);
+  const double rb = ndot3(r, b);
+  for (int i = 0; i < 3; ++i) r[i] = da(r[i], -dm(rb, b[i]));
+  const double rn = sqrt(ndot3(r, r));
+  for (int i = 0; i < 3; ++i) r[i] = r[i] / rn;
+  const double v2[3] = {da(dm(b[1], r[2]), -dm(b[2], r[1])), da(dm(b[2], r[0]), -dm(b[0], r[2])),
+                        da(dm(b[0], r[1]), -dm(b[1], r[0]))};
+  double dI[2];
+  for (int k = 0; k < 2; ++k) {
+    const double* v = k == 0 ? r : v2;
+    const double xp[3] = {da(X[0], dm(d, v[0])), da(X[1], dm(d, v[1])), da(X[2], dm(d, v[2]))};
+    const double xm[3] = {da(X[0], -dm(d, v[0])), da(X[1], -dm(d, v[1])), da(X[2], -dm(d, v[2]))};
+    const double I1 = fl_eye<M>(f, t, xp, Bm, flres, scratch, cap);
+    const double I2 = fl_eye<M>(f, t, xm, Bm, flres, scratch, cap);
+    if (I1 == 0.0) dI[k] = da(fl_eye<M>(f, t, X, Bm, flres, scratch, cap), -I2) / d;
+    else if (I2 == 0.0) dI[k] = da(I1, -fl_eye<M>(f, t, X, Bm, flres, scratch, cap)) / d;
+    else dI[k] = da(I1, -I2) / (2.0 * d);
+  }
+  for (int i = 0; i < 3; ++i) out[i] = da(dm(dI[0], r[i]), dm(dI[1], v2[i]));
 }
 
 // GuidingCenter.bounceperiod (GuidingCenter.py:593-606) at state (x, y, z, ppar).

@@ -1,5 +1,6 @@
 // inst_body.cuh -- instantiates every kernel for one field model. Included by
 // inst_model<k>.cu with RAPT_MODEL defined, so the models compile in parallel.
+#include "bc_kernels.cuh"
 #include "dense_kernels.cuh"
 #include "eval_kernels.cuh"
 #include "fp32_kernels.cuh"
@@ -107,6 +108,31 @@ cudaError_t bounce_period(const FieldP& f, double flres, int64_t n, const double
   k_bounce_period<kM><<<(unsigned)((n + 63) / 64), 64, 0, s>>>(f, flres, n, in, out, scratch, stride, cap);
   return cudaGetLastError();
 }
+cudaError_t bc_start(const FieldP& f, double flres, int64_t n, const double* st, const double* cst, double delta,
+                     double bctimestep, double* plan, int32_t* status, double* scratch, long long stride, int cap,
+                     cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_bc_start<kM><<<(unsigned)((n + 63) / 64), 64, 0, s>>>(f, flres, n, st, cst, delta, bctimestep, plan, status,
+                                                          scratch, stride, cap);
+  return cudaGetLastError();
+}
+cudaError_t bc_interval(const FieldP& f, const KParams& P, int64_t n, double* st, const double* cst,
+                        const double* plan, double d, int64_t j, double* rows, int max_rows, int32_t* nrows,
+                        int32_t* status, int64_t* counters, double* scratch, long long stride, int cap,
+                        cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_bc_interval<kM><<<(unsigned)((n + 63) / 64), 64, 0, s>>>(f, P, n, st, cst, plan, d, j, rows, max_rows, nrows,
+                                                             status, counters, scratch, stride, cap);
+  return cudaGetLastError();
+}
+cudaError_t bc_eval(const FieldP& f, double flres, int what, int64_t n, const double* tpos, const double* Bm,
+                    double d, const double* cst, double* out, double* scratch, long long stride, int cap,
+                    cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_bc_eval<kM><<<(unsigned)((n + 63) / 64), 64, 0, s>>>(f, flres, what, n, tpos, Bm, d, cst, out, scratch, stride,
+                                                         cap);
+  return cudaGetLastError();
+}
 cudaError_t adaptive_init(const DevEnsemble& E, const KParams& P, cudaStream_t s) {
   if (E.n <= 0) return cudaSuccess;
   k_adaptive_init<kM><<<(unsigned)((E.n + 127) / 128), 128, 0, s>>>(E, P);
@@ -145,5 +171,8 @@ void RAPT_CAT(register_model_, RAPT_MODEL)(ModelTable* t) {
   t->bounce_period = bounce_period;
   t->gc_dense = launch_gc_dense;
   t->occ_gc_dense = occ_gc_dense;
+  t->bc_start = bc_start;
+  t->bc_interval = bc_interval;
+  t->bc_eval = bc_eval;
 }
 }  // namespace rapt

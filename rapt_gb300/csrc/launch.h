@@ -20,6 +20,16 @@ using FieldEvalFn = cudaError_t (*)(const FieldP& f, int what, int64_t n, const 
 using RhsEvalFn = cudaError_t (*)(const KParams& P, int mode, int64_t n, const double* state, const double* mass,
                                   const double* charge, const double* v, double* out, cudaStream_t s);
 using AdaptiveInitFn = cudaError_t (*)(const DevEnsemble& E, const KParams& P, cudaStream_t s);
+using BcStartFn = cudaError_t (*)(const FieldP& f, double flres, int64_t n, const double* st, const double* cst,
+                                  double delta, double bctimestep, double* plan, int32_t* status, double* scratch,
+                                  long long stride, int cap, cudaStream_t s);
+using BcIntervalFn = cudaError_t (*)(const FieldP& f, const KParams& P, int64_t n, double* st, const double* cst,
+                                     const double* plan, double d, int64_t j, double* rows, int max_rows,
+                                     int32_t* nrows, int32_t* status, int64_t* counters, double* scratch,
+                                     long long stride, int cap, cudaStream_t s);
+using BcEvalFn = cudaError_t (*)(const FieldP& f, double flres, int what, int64_t n, const double* tpos,
+                                 const double* Bm, double d, const double* cst, double* out, double* scratch,
+                                 long long stride, int cap, cudaStream_t s);
 using BounceFn = cudaError_t (*)(const FieldP& f, double flres, int64_t n, const double* in, double* out,
                                  double* scratch, long long stride, int cap, cudaStream_t s);
 
@@ -40,6 +50,9 @@ struct ModelTable {
   BounceFn bounce_period;
   LaunchFn gc_dense;  // DOPRI5 guiding centres with dense output (rapt_config.dense_output)
   OccFn occ_gc_dense;
+  BcStartFn bc_start;        // BounceCenter.advance: cadence and row count
+  BcIntervalFn bc_interval;  // BounceCenter.advance: one output interval of every tracer
+  BcEvalFn bc_eval;          // second invariant, its gradient, the bounce-averaged drift
 };
 
 // MLP kernels (mlp.cu); packed BF16 weights take kMlpPackedWords u32

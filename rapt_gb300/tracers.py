@@ -429,6 +429,127 @@ def _estimate_rows(kind, tracers, delta):
     return n
 
 
+# ============================================================== BounceCenter
+class BounceCenter(_Pickle):
+    """Bounce-averaged tracer, rapt/BounceCenter.py:15-316, advanced on the GPU.
+
+    The drift gamma m v^2 / (q S_b |B|^2) (grad I x B) takes five field-line
+    traces per right-hand side (the half-bounce path and four second-invariant
+    integrals); the GPU runs one tracer per thread. Static fields only, as in the
+    reference. Kept from the reference: the constructor hands the pitch angle in
+    degrees to np.cos (BounceCenter.py:104), and advance() stamps each row with
+    the time its interval began. The reference's second-invariant integral raises
+    NameError below 70 degrees equatorial pitch angle (flutils.py:130); here that
+    range is served by the same spline method. isequatorial=True fails in the
+    reference (BounceCenter.py:238-239) and raises NotImplementedError here.
+    """
+
+    def __init__(self, pos=[], v=None, t0=0, pa=None, mass=None, charge=None, field=None):
+        self.pos = pos
+        self.v = v
+        self.t0 = t0
+        self.tcur = t0
+        self.mass = mass
+        self.charge = charge
+        self.field = field
+        self.isequatorial = False
+        if not field.static:
+            raise RuntimeError("BounceCenter does not work with nonstatic fields or electric fields.")
+        self.pa = pa
+        if not (len(pos) == 0 or v is None or pa is None):
+            self.trajectory = np.reshape(np.concatenate(([t0], pos)), (1, 4))
+            self.mu = ru.magnetic_moment(t0, pos, self.v * np.cos(self.pa), self.v, field, mass)
+            assert self.mu > 0
+
+    def _Bm(self):
+        gamma = 1.0 / np.sqrt(1 - (self.v / c) ** 2)
+        return self.mass * gamma ** 2 * self.v ** 2 / (2 * self.mu)
+
+    def _v_grad(self, tpos):
+        """BounceCenter.py:120-139."""
+        gamma = 1.0 / np.sqrt(1 - (self.v / c) ** 2)
+        Bvec = self.field.B(tpos)
+        gB = self.field.gradB(tpos)
+        return self.mu * np.cross(Bvec, gB) / (self.charge * gamma * np.dot(Bvec, Bvec))
+
+    def _v_inert(self, tpos):
+        """BounceCenter.py:141-172."""
+        vg = self._v_grad(tpos)
+        vgmag = np.sqrt(np.dot(vg, vg))
+        vgdir = np.zeros(4)
+        vgdir[0] = tpos[0]
+        vgdir[1:] = vg / vgmag
+        d = self.field.gradientstepsize
+        v1 = self._v_grad(tpos - d * vgdir)
+        v2 = self._v_grad(tpos + d * vgdir)
+        Bvec = self.field.B(tpos)
+        return self.mass * vgmag / (self.charge * np.dot(Bvec, Bvec) * 2 * d) * np.cross(Bvec, v2 - v1)
+
+    def drift(self, tpos):
+        """The bounce-averaged drift velocity (the right-hand side of advance)."""
+        ctx = N.default_context()
+        self.field.bind(ctx)
+        ctx.set_config(**_config())
+        return ctx.bc_eval("drift", tpos, self._Bm(), _params()["eyegradientstep"],
+                           [self.v, self.mu, self.mass, self.charge])[0]
+
+    def advance(self, delta):
+        """BounceCenter.advance (BounceCenter.py:214-252), on the GPU."""
+        advance_batch([self], delta)
+
+    def gett(self):
+        return self.trajectory[:, 0]
+
+    def getx(self):
+        return self.trajectory[:, 1]
+
+    def gety(self):
+        return self.trajectory[:, 2]
+
+    def getz(self):
+        return self.trajectory[:, 3]
+
+    def getr(self):
+        return np.sqrt(self.getx() ** 2 + self.gety() ** 2 + self.getz() ** 2)
+
+    def gettheta(self):
+        return np.arctan2(self.gety(), self.getx())
+
+    def getphi(self):
+        return np.arccos(self.getz() / self.getr())
+
+    def getB(self):
+        return np.asarray(self.field.magB(self.trajectory[:, :4]), float)
+
+
+def _advance_bc(tracers, delta):
+    if any(t.isequatorial for t in tracers):
+        raise NotImplementedError("isequatorial bounce centres fail in the reference (BounceCenter.py:238-239)")
+    p = _params()
+    field = tracers[0].field
+    ctx = N.default_context()
+    field.bind(ctx)
+    ctx.set_config(**_config())
+    n = len(tracers)
+    delta = np.broadcast_to(np.asarray(delta, float), (n,))
+    if np.any(delta != delta[0]):
+        raise ValueError("BounceCenter batches share one delta")
+    st0 = np.array([[*t.trajectory[-1, :4], t.tcur] for t in tracers])
+    cst = np.array([[t.v, t.mu, t.mass, t.charge] for t in tracers])
+    max_rows = 64
+    for _ in range(2):
+        st, rows, nr, status, cnt = ctx.bc_advance(st0.copy(), cst, delta[0], p["BCtimestep"],
+                                                   p["eyegradientstep"], max_rows)
+        if nr.max() <= max_rows:
+            break
+        max_rows = int(nr.max())  # rerun from the same start with room for every row
+    for i, t in enumerate(tracers):
+        if nr[i]:
+            t.trajectory = np.vstack((t.trajectory, rows[i, :nr[i]]))
+        t.tcur = st[i, 4]
+    return {"raised": np.zeros(n, bool), "stats": {"counters": cnt}, "status": status}
+
+
 def _raise_if_left_grid(res):
     # a Grid field evaluated outside its grid: the reference's interpolator raises
     # ValueError from inside the step (fields.py:733-737); the rows before it stay
@@ -446,6 +567,8 @@ def advance_batch(tracers, delta, eom="TaoChanBrizardEOM", tableau=0, verbose=Fa
     field = tracers[0].field
     if any(type(t) is not cls or t.field is not field for t in tracers):
         raise ValueError("advance_batch needs tracers of one class sharing one field object")
+    if cls is BounceCenter:
+        return _advance_bc(tracers, delta)
     kind = {Particle: N.KIND_PARTICLE, GuidingCenter: N.KIND_GC, Adaptive: N.KIND_ADAPTIVE}[cls]
     n = len(tracers)
     delta = np.broadcast_to(np.asarray(delta, float), (n,)).copy()

@@ -216,3 +216,19 @@ def gc_grid(n=262144, seed=0):
     w["params"] = dict(rtol=1e-6, atol=1e-6, gctimestep=0.5)
     w["t0"] = 0.5
     return w
+
+
+def bc_drift(n=65536, seed=0):
+    """Bounce centres (BounceCenter): protons in the DoubleDipole field,
+    equatorial start at L uniform 4-7, MLT uniform 0-24 h, KE log-uniform
+    0.5-5 MeV, equatorial pitch angle uniform 70-88 deg (the range where the
+    reference's second-invariant integral runs), BCtimestep 0.1 bounce periods,
+    eyegradientstep 0.03 Re, SciPy's default tolerances. mu from the pitch angle
+    (gamma^2 m v^2 sin^2(a) / (2 |B|))."""
+    rng = np.random.default_rng(seed)
+    pos = _equatorial(rng, n, 4.0, 7.0)
+    ke = 10 ** rng.uniform(np.log10(0.5 * MeV), np.log10(5 * MeV), n)
+    eqpa = rng.uniform(70.0, 88.0, n)
+    return dict(name="bc_drift", field=("DoubleDipole", {}), kind="bc", pos=pos, ke=ke, eqpa=eqpa,
+                v=speed_from_ke(ke, m_pr), mass=np.full(n, m_pr), charge=np.full(n, e),
+                params=dict(rtol=1.49012e-8, atol=1.49012e-8, bctimestep=0.1, eyegradientstep=0.03 * Re))

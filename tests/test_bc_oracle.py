@@ -1,0 +1,68 @@
+"""The second invariant and BounceCenter (rapt/flutils.py:65-229,
+rapt/BounceCenter.py) in the CPU oracle, pinned against
+tests/golden/bc_golden.npz from the unmodified reference."""
+import os
+
+import numpy as np
+
+GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "bc_golden.npz"))
+Re = 6378137.0
+NAMES = {0: "EarthDipole", 1: "DoubleDipole"}
+
+
+def test_eye_matches_reference(oracle):
+    for mid, L, eqpa, Bm, ref, dip in GOLD["eye"]:
+        f = oracle.field(NAMES[int(mid)])
+        tpos = np.array([0.0, L * Re, 0.0, 0.0])
+        got = oracle.eye(f, tpos, Bm)
+        if np.isnan(ref):  # the reference raises NameError below 70 degrees
+            assert eqpa < 70 and np.isnan(got)
+            continue
+        assert abs(got - ref) <= 1e-12 * abs(ref), (L, eqpa, got, ref)
+        # the converged integral of the same spline: within QAGS's epsrel 1e-4
+        conv = oracle.eye(f, tpos, Bm, quad=1)
+        assert abs(conv - ref) <= 2e-5 * abs(ref), (L, eqpa, conv, ref)
+
+
+def test_eye_against_the_dipole_formula(oracle):
+    """Every pitch angle (including those where the reference's field-line path
+    raises) against utils.dipoleI, the reference's closed form for a dipole:
+    the difference is the trace's discretisation."""
+    for mid, L, eqpa, Bm, ref, dip in GOLD["eye"]:
+        if int(mid) != 0:
+            continue
+        got = oracle.eye(oracle.field("EarthDipole"), np.array([0.0, L * Re, 0.0, 0.0]), Bm, quad=1)
+        assert abs(got - dip) <= 3e-6 * dip, (L, eqpa, got, dip)
+
+
+def test_gradI_matches_reference(oracle):
+    for mid, x, y, z, Bm, gx, gy, gz in GOLD["gradI"]:
+        f = oracle.field(NAMES[int(mid)])
+        got = oracle.gradI(f, np.array([0.0, x, y, z]), Bm, 0.03 * Re)
+        ref = np.array([gx, gy, gz])
+        assert np.allclose(got, ref, rtol=1e-9, atol=1e-9 * np.abs(ref).max()), (got, ref)
+
+
+def test_bounce_center_trajectories_match_reference(oracle):
+    for mid, v, pa, mass, charge, mu, bp, delta, tcur in GOLD["bc_cases"]:
+        name = NAMES[int(mid)]
+        f = oracle.field(name)
+        pos = np.array([6 * Re, 0.0, 0.0])
+        assert abs(oracle.bc_mu(f, pos, v, pa, 0.0, mass) - mu) <= 1e-15 * mu
+        state = np.array([0.0, *pos, 0.0])
+        cfg = oracle.config(rtol=1.49012e-8, atol=1.49012e-8)
+        st, rows, cnt = oracle.bc_advance(f, cfg, state, v, mu, mass, charge, delta, 0.1, 0.03 * Re)
+        ref = GOLD["bc_%s_rows" % name]
+        assert st == 0 and rows.shape == ref[1:].shape, (st, rows.shape)
+        # stamps np.arange(tcur, tcur + delta, dt), dt from the bounce period's QAGS
+        assert np.allclose(rows[:, 0], ref[1:, 0], rtol=1e-12, atol=0)
+        assert np.allclose(rows[:, 1:], ref[1:, 1:], rtol=1e-10, atol=1e-10 * Re), np.abs(rows - ref[1:]).max()
+        assert abs(state[4] - tcur) <= 1e-12 * tcur
+
+
+def test_bounce_center_needs_a_static_field():
+    import pytest
+
+    import rapt_gb300 as R
+    with pytest.raises(RuntimeError):
+        R.BounceCenter([6 * Re, 0, 0], 1e7, 0, 80, 1.672621777e-27, 1.602176565e-19, R.fields.VarEarthDipole())
