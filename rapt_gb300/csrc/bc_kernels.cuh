@@ -28,12 +28,14 @@ struct BcRHS {
   double Bm, kdrift, d, flres;  // kdrift = gamma m v^2 / q
   double* scratch;
   int cap;
+  int32_t* flag;  // set where a value is not finite (the host reruns the tracer with full trace slots)
   __device__ void operator()(double t, const double* Y, double* o) const {
     double B[3], gI[3];
     Field<M>::B(f, t, Y[0], Y[1], Y[2], B);
     const double magBsq = ndot3(B, B);
     const double Sb = fl_halfbouncepath<M>(f, t, Y, Bm, flres, scratch, cap);
     fl_gradI<M>(f, t, Y, Bm, d, flres, scratch, cap, gI);
+    if (flag && !(isfinite(Sb) && isfinite(gI[0]) && isfinite(gI[1]) && isfinite(gI[2]))) *flag = 1;
     const double k = kdrift / dm(Sb, magBsq);
     o[0] = dm(k, da(dm(gI[1], B[2]), -dm(gI[2], B[1])));
     o[1] = dm(k, da(dm(gI[2], B[0]), -dm(gI[0], B[2])));
@@ -47,8 +49,8 @@ __device__ __forceinline__ double bc_gamma(double v) { return 1.0 / sqrt(1.0 - (
 // st[5] = (t, x, y, z, tcur); plan[4] = (Bm, dt, K, arange step).
 template <int M>
 __global__ void k_bc_start(FieldP f, double flres, int64_t n, const double* st, const double* cst, double delta,
-                           double bctimestep, double* plan, int32_t* status, double* scratch, long long stride,
-                           int cap) {
+                           double bctimestep, double* plan, int32_t* status, int32_t* flag, double* scratch,
+                           long long stride, int cap) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const double* s = st + 5 * k;
@@ -63,6 +65,7 @@ __global__ void k_bc_start(FieldP f, double flres, int64_t n, const double* st, 
   p[1] = dt;
   if (!(dt > 0.0) || !isfinite(dt)) {
     status[k] = RAPT_ST_FIELDLINE;
+    if (flag) flag[k] = 1;
     p[2] = 0.0;
     return;
   }
@@ -79,7 +82,7 @@ template <int M>
 __global__ void __launch_bounds__(64) k_bc_interval(FieldP f, KParams P, int64_t n, double* st, const double* cst,
                                                     const double* plan, double d, int64_t j, double* rows,
                                                     int max_rows, int32_t* nrows, int32_t* status, int64_t* counters,
-                                                    double* scratch, long long stride, int cap) {
+                                                    int32_t* flag, double* scratch, long long stride, int cap) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const double* p = plan + 4 * k;
@@ -87,7 +90,8 @@ __global__ void __launch_bounds__(64) k_bc_interval(FieldP f, KParams P, int64_t
   double* s = st + 5 * k;
   const double v = cst[4 * k], mass = cst[4 * k + 2], charge = cst[4 * k + 3];
   const double gamma = bc_gamma(v);
-  const BcRHS<M> rhs{f, p[0], dm(dm(dm(gamma, mass), v), v) / charge, d, P.flres, scratch + (size_t)k * stride, cap};
+  const BcRHS<M> rhs{f, p[0], dm(dm(dm(gamma, mass), v), v) / charge, d, P.flres, scratch + (size_t)k * stride, cap,
+                     flag ? flag + k : nullptr};
   const double dt = p[1];
   double rt = s[0];
   double y[3] = {s[1], s[2], s[3]}, k1[3];
@@ -168,7 +172,7 @@ __global__ void k_bc_eval(FieldP f, double flres, int what, int64_t n, const dou
   } else {
     const double v = cst[4 * k], mass = cst[4 * k + 2], charge = cst[4 * k + 3];
     const double gamma = bc_gamma(v);
-    const BcRHS<M> rhs{f, Bm[k], dm(dm(dm(gamma, mass), v), v) / charge, d, flres, scr, cap};
+    const BcRHS<M> rhs{f, Bm[k], dm(dm(dm(gamma, mass), v), v) / charge, d, flres, scr, cap, nullptr};
     rhs(tp[0], X, o);
   }
 }

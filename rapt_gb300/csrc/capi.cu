@@ -1050,9 +1050,69 @@ static int ensure_fl_scratch(Ctx* c, size_t n) {
   return RAPT_OK;
 }
 
-// tracers per BounceCenter pass: their trace scratch (64 KB each, one slot per
-// thread) is 512 MiB, so that the passes' scratch traffic stays mostly in L2
-constexpr int64_t kBcChunk = 8192;
+// BounceCenter passes. A first pass gives each thread a small trace slot
+// (kBcCapSmall points per direction: 8 KB; the lines of the pitch angles where
+// the reference's second-invariant integral runs have a few tens), 16,384
+// tracers at a time, so that the slots (128 MiB) stay in L2; a tracer whose
+// right-hand side met a non-finite value (a trace that did not fit, among
+// others) is then rerun from its start with full slots (kFieldlineCap points,
+// 64 KB), 2,048 at a time. The rerun reproduces a full-slot run exactly.
+constexpr int kBcCapSmall = 128;
+constexpr int64_t kBcChunkSmall = 16384, kBcChunkFull = 2048;
+
+static int bc_pass(Ctx* c, int64_t n, double* state, const double* cst, double delta, double bctimestep,
+                   double eyegradientstep, double* rows, int32_t max_rows, int32_t* nrows, int32_t* status,
+                   int64_t* counters, int32_t* flagged, int cap, int64_t chunk_max) {
+  const long long stride = 8LL * cap;
+  const int64_t chunk = std::min<int64_t>(n, chunk_max);
+  int rc = ensure_fl_scratch(c, (size_t)chunk * (size_t)cap / kFieldlineCap + 1);
+  if (rc) return rc;
+  KParams P = make_params(c, RAPT_KIND_GC);
+  const ModelTable& T = c->tab[c->field.model];
+  // device block per chunk: st 5 | cst 4 | plan 4 | counters 4 (int64) | status, nrows, flag (int32) | rows
+  const size_t C = (size_t)chunk, R = (size_t)max_rows;
+  rc = ensure_tmp(c, C * (17 * 8 + 4 * 4) + C * R * 4 * 8);
+  if (rc) return rc;
+  char* base = static_cast<char*>(c->tmp);
+  double* d_st = reinterpret_cast<double*>(base);
+  double* d_cst = d_st + 5 * C;
+  double* d_plan = d_cst + 4 * C;
+  int64_t* d_cnt = reinterpret_cast<int64_t*>(d_plan + 4 * C);
+  int32_t* d_status = reinterpret_cast<int32_t*>(d_cnt + 4 * C);
+  int32_t* d_nrows = d_status + C;
+  int32_t* d_flag = d_nrows + C;
+  double* d_rows = reinterpret_cast<double*>(d_flag + C + C);  // 17C doubles + 4C int32: 8-byte aligned
+  std::vector<double> plan;
+  for (int64_t k0 = 0; k0 < n; k0 += chunk) {
+    const int64_t m = std::min(chunk, n - k0);
+    const size_t M = (size_t)m;
+    CK(cudaMemcpyAsync(d_st, state + 5 * k0, M * 5 * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d_cst, cst + 4 * k0, M * 4 * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(d_cnt, 0, M * 4 * 8, c->stream));
+    CK(cudaMemsetAsync(d_nrows, 0, M * 4, c->stream));
+    CK(cudaMemsetAsync(d_flag, 0, M * 4, c->stream));
+    CK(T.bc_start(c->field, c->cfg.fieldlineresolution, m, d_st, d_cst, delta, bctimestep, d_plan, d_status,
+                  d_flag, c->fl_scratch, stride, cap, c->stream));
+    plan.resize(M * 4);
+    CK(cudaMemcpyAsync(plan.data(), d_plan, M * 4 * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    double kmax = 0.0;
+    for (size_t i = 0; i < M; ++i) kmax = std::max(kmax, plan[4 * i + 2]);
+    if (kmax > 1e7) return fail(c, RAPT_ERR_INVALID, "more than 1e7 rows per BounceCenter (delta / dt)");
+    for (int64_t j = 0; j < (int64_t)kmax; ++j)
+      CK(T.bc_interval(c->field, P, m, d_st, d_cst, d_plan, eyegradientstep, j, d_rows, max_rows, d_nrows, d_status,
+                       d_cnt, d_flag, c->fl_scratch, stride, cap, c->stream));
+    CK(cudaMemcpyAsync(state + 5 * k0, d_st, M * 5 * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(status + k0, d_status, M * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(nrows + k0, d_nrows, M * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (flagged) CK(cudaMemcpyAsync(flagged + k0, d_flag, M * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (max_rows > 0)
+      CK(cudaMemcpyAsync(rows + (size_t)k0 * R * 4, d_rows, M * R * 4 * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(counters + 4 * k0, d_cnt, M * 4 * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return RAPT_OK;
+}
 
 int rapt_bc_advance(void* ctx, int64_t n, double* state, const double* cst, double delta, double bctimestep,
                     double eyegradientstep, double* rows, int32_t max_rows, int32_t* nrows, int32_t* status,
@@ -1067,51 +1127,39 @@ int rapt_bc_advance(void* ctx, int64_t n, double* state, const double* cst, doub
     return fail(c, RAPT_ERR_INVALID, "bad BCtimestep, eyegradientstep or delta");
   if (n == 0) return RAPT_OK;
   CK(cudaSetDevice(c->device));
-  const long long stride = 8LL * kFieldlineCap;
-  const int64_t chunk = std::min<int64_t>(n, kBcChunk);
-  int rc = ensure_fl_scratch(c, (size_t)chunk);
+  const size_t N = (size_t)n, R = (size_t)max_rows;
+  const std::vector<double> start(state, state + 5 * N);
+  std::vector<int32_t> flagged(N, 0);
+  std::vector<int64_t> cnt(4 * N, 0);
+  int rc = bc_pass(c, n, state, cst, delta, bctimestep, eyegradientstep, rows, max_rows, nrows, status, cnt.data(),
+                   flagged.data(), kBcCapSmall, kBcChunkSmall);
   if (rc) return rc;
-  KParams P = make_params(c, RAPT_KIND_GC);
-  const ModelTable& T = c->tab[c->field.model];
-  // device block per pass: st 5 | cst 4 | plan 4 | counters 4 (int64) | status, nrows (int32) | rows
-  const size_t C = (size_t)chunk, R = (size_t)max_rows;
-  rc = ensure_tmp(c, C * (17 * 8 + 2 * 4) + C * R * 4 * 8);
-  if (rc) return rc;
-  char* base = static_cast<char*>(c->tmp);
-  double* d_st = reinterpret_cast<double*>(base);
-  double* d_cst = d_st + 5 * C;
-  double* d_plan = d_cst + 4 * C;
-  int64_t* d_cnt = reinterpret_cast<int64_t*>(d_plan + 4 * C);
-  int32_t* d_status = reinterpret_cast<int32_t*>(d_cnt + 4 * C);
-  int32_t* d_nrows = d_status + C;
-  double* d_rows = reinterpret_cast<double*>(d_nrows + C);  // 17C doubles + 2C int32: 8-byte aligned
-  std::vector<double> plan;
-  for (int64_t k0 = 0; k0 < n; k0 += chunk) {
-    const int64_t m = std::min(chunk, n - k0);
-    const size_t M = (size_t)m;
-    CK(cudaMemcpyAsync(d_st, state + 5 * k0, M * 5 * 8, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(d_cst, cst + 4 * k0, M * 4 * 8, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemsetAsync(d_cnt, 0, M * 4 * 8, c->stream));
-    CK(cudaMemsetAsync(d_nrows, 0, M * 4, c->stream));
-    CK(T.bc_start(c->field, c->cfg.fieldlineresolution, m, d_st, d_cst, delta, bctimestep, d_plan, d_status,
-                  c->fl_scratch, stride, kFieldlineCap, c->stream));
-    plan.resize(M * 4);
-    CK(cudaMemcpyAsync(plan.data(), d_plan, M * 4 * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    double kmax = 0.0;
-    for (size_t i = 0; i < M; ++i) kmax = std::max(kmax, plan[4 * i + 2]);
-    if (kmax > 1e7) return fail(c, RAPT_ERR_INVALID, "more than 1e7 rows per BounceCenter (delta / dt)");
-    for (int64_t j = 0; j < (int64_t)kmax; ++j)
-      CK(T.bc_interval(c->field, P, m, d_st, d_cst, d_plan, eyegradientstep, j, d_rows, max_rows, d_nrows, d_status,
-                       d_cnt, c->fl_scratch, stride, kFieldlineCap, c->stream));
-    CK(cudaMemcpyAsync(state + 5 * k0, d_st, M * 5 * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(status + k0, d_status, M * 4, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(nrows + k0, d_nrows, M * 4, cudaMemcpyDeviceToHost, c->stream));
-    if (max_rows > 0)
-      CK(cudaMemcpyAsync(rows + (size_t)k0 * R * 4, d_rows, M * R * 4 * 8, cudaMemcpyDeviceToHost, c->stream));
-    if (counters) CK(cudaMemcpyAsync(counters + 4 * k0, d_cnt, M * 4 * 8, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
+  std::vector<int64_t> redo;
+  for (size_t i = 0; i < N; ++i)
+    if (flagged[i]) redo.push_back((int64_t)i);
+  if (!redo.empty()) {
+    const size_t m = redo.size();
+    std::vector<double> st2(5 * m), cst2(4 * m), rows2(m * R * 4);
+    std::vector<int32_t> nr2(m), status2(m);
+    std::vector<int64_t> cnt2(4 * m);
+    for (size_t a = 0; a < m; ++a) {
+      std::memcpy(&st2[5 * a], &start[5 * redo[a]], 5 * 8);
+      std::memcpy(&cst2[4 * a], cst + 4 * redo[a], 4 * 8);
+    }
+    rc = bc_pass(c, (int64_t)m, st2.data(), cst2.data(), delta, bctimestep, eyegradientstep,
+                 R ? rows2.data() : nullptr, max_rows, nr2.data(), status2.data(), cnt2.data(), nullptr,
+                 kFieldlineCap, kBcChunkFull);
+    if (rc) return rc;
+    for (size_t a = 0; a < m; ++a) {
+      const size_t k = (size_t)redo[a];
+      std::memcpy(state + 5 * k, &st2[5 * a], 5 * 8);
+      if (R) std::memcpy(rows + k * R * 4, &rows2[a * R * 4], R * 4 * 8);
+      nrows[k] = nr2[a];
+      status[k] = status2[a];
+      std::memcpy(&cnt[4 * k], &cnt2[4 * a], 4 * 8);
+    }
   }
+  if (counters) std::memcpy(counters, cnt.data(), 4 * N * 8);
   return RAPT_OK;
 }
 
@@ -1124,7 +1172,7 @@ int rapt_bc_eval(void* ctx, int what, int64_t n, const double* tpos, const doubl
   if (n == 0) return RAPT_OK;
   CK(cudaSetDevice(c->device));
   const long long stride = 8LL * kFieldlineCap;
-  const int64_t chunk = std::min<int64_t>(n, kBcChunk);
+  const int64_t chunk = std::min<int64_t>(n, kBcChunkFull);
   int rc = ensure_fl_scratch(c, (size_t)chunk);
   if (rc) return rc;
   const size_t C = (size_t)chunk;

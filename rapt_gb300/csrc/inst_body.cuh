@@ -109,20 +109,20 @@ cudaError_t bounce_period(const FieldP& f, double flres, int64_t n, const double
   return cudaGetLastError();
 }
 cudaError_t bc_start(const FieldP& f, double flres, int64_t n, const double* st, const double* cst, double delta,
-                     double bctimestep, double* plan, int32_t* status, double* scratch, long long stride, int cap,
-                     cudaStream_t s) {
+                     double bctimestep, double* plan, int32_t* status, int32_t* flag, double* scratch,
+                     long long stride, int cap, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   k_bc_start<kM><<<(unsigned)((n + 63) / 64), 64, 0, s>>>(f, flres, n, st, cst, delta, bctimestep, plan, status,
-                                                          scratch, stride, cap);
+                                                          flag, scratch, stride, cap);
   return cudaGetLastError();
 }
 cudaError_t bc_interval(const FieldP& f, const KParams& P, int64_t n, double* st, const double* cst,
                         const double* plan, double d, int64_t j, double* rows, int max_rows, int32_t* nrows,
-                        int32_t* status, int64_t* counters, double* scratch, long long stride, int cap,
-                        cudaStream_t s) {
+                        int32_t* status, int64_t* counters, int32_t* flag, double* scratch, long long stride,
+                        int cap, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   k_bc_interval<kM><<<(unsigned)((n + 63) / 64), 64, 0, s>>>(f, P, n, st, cst, plan, d, j, rows, max_rows, nrows,
-                                                             status, counters, scratch, stride, cap);
+                                                             status, counters, flag, scratch, stride, cap);
   return cudaGetLastError();
 }
 cudaError_t bc_eval(const FieldP& f, double flres, int what, int64_t n, const double* tpos, const double* Bm,

@@ -21,12 +21,12 @@ using RhsEvalFn = cudaError_t (*)(const KParams& P, int mode, int64_t n, const d
                                   const double* charge, const double* v, double* out, cudaStream_t s);
 using AdaptiveInitFn = cudaError_t (*)(const DevEnsemble& E, const KParams& P, cudaStream_t s);
 using BcStartFn = cudaError_t (*)(const FieldP& f, double flres, int64_t n, const double* st, const double* cst,
-                                  double delta, double bctimestep, double* plan, int32_t* status, double* scratch,
-                                  long long stride, int cap, cudaStream_t s);
+                                  double delta, double bctimestep, double* plan, int32_t* status, int32_t* flag,
+                                  double* scratch, long long stride, int cap, cudaStream_t s);
 using BcIntervalFn = cudaError_t (*)(const FieldP& f, const KParams& P, int64_t n, double* st, const double* cst,
                                      const double* plan, double d, int64_t j, double* rows, int max_rows,
-                                     int32_t* nrows, int32_t* status, int64_t* counters, double* scratch,
-                                     long long stride, int cap, cudaStream_t s);
+                                     int32_t* nrows, int32_t* status, int64_t* counters, int32_t* flag,
+                                     double* scratch, long long stride, int cap, cudaStream_t s);
 using BcEvalFn = cudaError_t (*)(const FieldP& f, double flres, int what, int64_t n, const double* tpos,
                                  const double* Bm, double d, const double* cst, double* out, double* scratch,
                                  long long stride, int cap, cudaStream_t s);
