@@ -231,7 +231,8 @@ int rapt_gc_bounce_period(void* ctx, int64_t n, const double* state, double* out
 
 /* --- BounceCenter (rapt/BounceCenter.py) and the second invariant ----------
  * BounceCenter.advance(delta) (BounceCenter.py:214-252) for n bounce centres at
- * once, one GPU thread each (field-line traces in a 64 KB scratch slot): the
+ * once, one GPU thread each (field-line traces in a per-thread scratch slot: 8 KB in passes of
+ * 16,384 tracers; a tracer that meets a non-finite value is rerun with 64 KB slots): the
  * drift gamma m v^2 / (q S_b |B|^2) (grad I x B) with S_b = halfbouncepath
  * and grad I = flutils.gradI (five field-line traces per right-hand side),
  * rows every bctimestep x the bounce period at the start, SciPy-dopri5
