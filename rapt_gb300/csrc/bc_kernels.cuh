@@ -17,11 +17,6 @@
 
 namespace rapt {
 
-// per-tracer constants: v, mu, mass, charge; derived: Bm, gamma m v^2 / q
-struct BcConst {
-  double v, mu, mass, charge;
-};
-
 template <int M>
 struct BcRHS {
   FieldP f;

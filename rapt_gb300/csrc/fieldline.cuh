@@ -180,8 +180,6 @@ struct DSpline2 {
 // yc holds the data on entry and the coefficients on exit; di, up scratch.
 static __device__ __noinline__ void spline2_solve(const double* x, double* yc, double* di, double* up, int n) {
   DSpline2 sp{x, yc, n};
-  double lo_prev = 0.0;
-  (void)lo_prev;
   // forward elimination row by row (the lower entry is formed when the row is built)
   for (int i = 0; i < n; ++i) {
     const int l = sp.find(x[i]);
