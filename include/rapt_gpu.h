@@ -112,9 +112,9 @@ typedef struct {
                                     bounceperiod() / bounceresolution (GuidingCenter.py:443-446) */
   double fieldlineresolution;    /* params["fieldlineresolution"] (fieldline.py:31-35) */
   int32_t dense_output;          /* 1: guiding centres integrate through each advance() call without restarting
-                                    at the output times (step <= the cadence) and output rows from DOPRI5's
-                                    order-4 continuous extension; plain form, DOPRI5 only. No reference
-                                    counterpart (the reference restarts SciPy's dopri5 per row) */
+                                    at the output times (steps up to 16 output intervals) and output rows from
+                                    DOPRI5's order-4 continuous extension; plain form, DOPRI5 only, max_rows >= 18.
+                                    No reference counterpart (the reference restarts SciPy's dopri5 per row) */
 } rapt_config;
 
 /* Host-side SoA view of an ensemble. Any pointer may be NULL on download to
@@ -250,9 +250,10 @@ int rapt_gc_bounce_period(void* ctx, int64_t n, const double* state, double* out
 int rapt_bc_advance(void* ctx, int64_t n, double* state, const double* cst, double delta, double bctimestep,
                     double eyegradientstep, double* rows, int32_t max_rows, int32_t* nrows, int32_t* status,
                     int64_t* counters);
-/* Checks at tpos[n][4] with mirror fields Bm[n]: what 0 flutils.eye (out[n][3],
- * first value), 1 flutils.gradI, 2 the bounce-averaged drift velocity (needs
- * cst[n][4] as above). NaN where a trace overflows or the reference raises. */
+/* Field-line quantities at tpos[n][4] with mirror fields Bm[n]: what 0
+ * flutils.eye (out[n][3], first value), 1 flutils.gradI, 2 the bounce-averaged
+ * drift velocity (needs cst[n][4] as above), 3 flutils.halfbouncepath (first
+ * value; flutils.py:254-316). NaN where a trace overflows or the reference raises. */
 int rapt_bc_eval(void* ctx, int what, int64_t n, const double* tpos, const double* Bm, double eyegradientstep,
                  const double* cst, double* out);
 

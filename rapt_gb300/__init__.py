@@ -46,4 +46,5 @@ params = {
 from . import fields, workloads  # noqa: E402
 from .ensemble import Ensemble  # noqa: E402
 from . import utils  # noqa: E402
+from . import flutils  # noqa: E402
 from .tracers import Adaptive, BounceCenter, GuidingCenter, Particle, advance_batch  # noqa: E402

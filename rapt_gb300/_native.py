@@ -217,7 +217,7 @@ class Context:
         Bm = np.ascontiguousarray(np.broadcast_to(np.asarray(Bm, float), (n,)))
         c = None if cst is None else np.ascontiguousarray(np.broadcast_to(np.asarray(cst, float), (n, 4)))
         out = np.zeros((n, 3))
-        what = {"eye": 0, "gradI": 1, "drift": 2}.get(what, what)
+        what = {"eye": 0, "gradI": 1, "drift": 2, "halfbouncepath": 3}.get(what, what)
         self.check(self.L.rapt_bc_eval(self.h, int(what), n, ptr(tpos), ptr(Bm), float(eyegradientstep), ptr(c),
                                        ptr(out)), "rapt_bc_eval")
         return out

@@ -148,8 +148,9 @@ __global__ void __launch_bounds__(64) k_bc_interval(FieldP f, KParams P, int64_t
   }
 }
 
-// Checks: what 0 the second invariant I, 1 grad I (3 values), 2 the drift
-// velocity (3 values) at tpos[n][4] with mirror fields Bm[n] (what 2: cst[n][4]).
+// what 0 the second invariant I, 1 grad I (3 values), 2 the drift velocity
+// (3 values), 3 the half-bounce path, at tpos[n][4] with mirror fields Bm[n]
+// (what 2: cst[n][4]).
 template <int M>
 __global__ void k_bc_eval(FieldP f, double flres, int what, int64_t n, const double* tpos, const double* Bm, double d,
                           const double* cst, double* out, double* scratch, long long stride, int cap) {
@@ -159,8 +160,9 @@ __global__ void k_bc_eval(FieldP f, double flres, int what, int64_t n, const dou
   const double X[3] = {tp[1], tp[2], tp[3]};
   double* scr = scratch + (size_t)k * stride;
   double* o = out + 3 * k;
-  if (what == 0) {
-    o[0] = fl_eye<M>(f, tp[0], X, Bm[k], flres, scr, cap);
+  if (what == 0 || what == 3) {
+    o[0] = what == 0 ? fl_eye<M>(f, tp[0], X, Bm[k], flres, scr, cap)
+                     : fl_halfbouncepath<M>(f, tp[0], X, Bm[k], flres, scr, cap);
     o[1] = o[2] = 0.0;
   } else if (what == 1) {
     fl_gradI<M>(f, tp[0], X, Bm[k], d, flres, scr, cap, o);

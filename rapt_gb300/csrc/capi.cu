@@ -1166,7 +1166,7 @@ int rapt_bc_advance(void* ctx, int64_t n, double* state, const double* cst, doub
 int rapt_bc_eval(void* ctx, int what, int64_t n, const double* tpos, const double* Bm, double eyegradientstep,
                  const double* cst, double* out) {
   Ctx* c = static_cast<Ctx*>(ctx);
-  if (!c || what < 0 || what > 2 || n < 0 || (n > 0 && (!tpos || !Bm || !out || (what == 2 && !cst))))
+  if (!c || what < 0 || what > 3 || n < 0 || (n > 0 && (!tpos || !Bm || !out || (what == 2 && !cst))))
     return RAPT_ERR_INVALID;
   if (!c->field_set) return fail(c, RAPT_ERR_STATE, "no field set");
   if (n == 0) return RAPT_OK;

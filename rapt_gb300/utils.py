@@ -7,6 +7,8 @@ import numpy as np
 
 c = 299792458
 e = 1.602176565e-19
+Re = 6378137  # rapt/__init__.py:11-12
+B0 = 3.07e-5
 
 
 def gamma(mass=0, **kwargs):
@@ -130,3 +132,35 @@ def GCtoFP(t, R, vp, speed, field, mass, charge, gyrophase=0):
     pos = R + rc * (np.cos(gyrophase) * u + np.sin(gyrophase) * w)
     vel = speed * (np.cos(pa) * b + s * np.sin(pa) * np.sin(gyrophase) * u - s * np.sin(pa) * np.cos(gyrophase) * w)
     return pos, vel
+
+
+def dipoleI(R0, Bm):
+    """The second invariant I = integral of sqrt(1 - B/Bm) ds between the mirror
+    points of the dipole line through the equator at R0 (rapt/utils.py:531-557):
+    on r = R0 cos^2(lat), B = B0 (Re/R0)^3 sqrt(1 + 3 sin^2) / cos^6 and
+    ds = R0 cos sqrt(1 + 3 sin^2) d(lat), integrated over latitude (host
+    quadrature: a closed-form helper, not the stepping path)."""
+    from scipy.integrate import quad
+    from scipy.optimize import brentq
+    Beq = B0 * (Re / R0) ** 3
+
+    def Bratio(lat):
+        s2 = np.sin(lat) ** 2
+        return Beq * np.sqrt(1 + 3 * s2) / np.cos(lat) ** 6 / Bm
+
+    if Beq >= Bm:
+        return 0.0
+    lat_m = brentq(lambda lat: Bratio(lat) - 1.0, 0.0, np.pi / 2 - 1e-9, xtol=1e-15, rtol=4 * np.finfo(float).eps)
+
+    def integrand(lat):
+        s2 = np.sin(lat) ** 2
+        return np.sqrt(max(1.0 - Bratio(lat), 0.0)) * R0 * np.cos(lat) * np.sqrt(1 + 3 * s2)
+
+    return 2 * quad(integrand, 0.0, lat_m, epsabs=0.0, epsrel=1e-12, limit=200)[0]
+
+
+def dipole_gradI(x, y, Bm, h):
+    """rapt/utils.py:559-581: central difference of dipoleI in the radial direction."""
+    r0 = np.sqrt(x ** 2 + y ** 2)
+    mag = (dipoleI(r0 + h, Bm) - dipoleI(r0 - h, Bm)) / (2 * h)
+    return mag * np.array((x, y, 0)) / r0

@@ -66,3 +66,14 @@ def test_bounce_center_needs_a_static_field():
     import rapt_gb300 as R
     with pytest.raises(RuntimeError):
         R.BounceCenter([6 * Re, 0, 0], 1e7, 0, 80, 1.672621777e-27, 1.602176565e-19, R.fields.VarEarthDipole())
+
+
+def test_dipole_closed_forms_match_reference():
+    """utils.dipoleI (rapt/utils.py:531-557) in the facade, integrated over
+    latitude, against the reference's values."""
+    from rapt_gb300 import utils as U
+    for mid, L, eqpa, Bm, ref, dip in GOLD["eye"]:
+        if int(mid) == 0:
+            assert abs(U.dipoleI(L * Re, Bm) - dip) <= 1e-11 * dip
+    g = U.dipole_gradI(5 * Re, 2 * Re, 4e-7, 0.03 * Re)
+    assert g[2] == 0 and np.isclose(g[1] / g[0], 0.4, rtol=1e-14) and g[0] > 0

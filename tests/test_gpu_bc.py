@@ -89,3 +89,28 @@ def test_bounce_center_object_api():
     assert abs(b.tcur - tcur) <= 1e-5 * tcur
     b.advance(delta)  # continues from trajectory[-1]
     assert b.trajectory.shape == (9, 4) and np.all(np.diff(b.gety()) < 0)
+
+
+def test_flutils_facade(oracle):
+    """rapt_gb300.flutils: the half-bounce path against the reference's golden
+    values and the oracle; eye and gradI through the object API."""
+    import rapt_gb300 as R
+    gold = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden.npz"))
+    for mid, L, pa, phi, Bm, Sb in gold["bounce_halfpath"]:
+        name = NAMES.get(int(mid))
+        if name is None:
+            continue
+        fld = getattr(R.fields, name)()
+        tpos = np.array([0.0, L * Re * np.cos(np.radians(phi)), L * Re * np.sin(np.radians(phi)), 0.0])
+        got = R.flutils.halfbouncepath(tpos, fld, Bm)
+        conv = oracle.halfbouncepath(oracle.field(name), tpos, Bm, quad=1)[0]
+        assert abs(got - conv) <= 1e-10 * conv and abs(got - Sb) <= 1e-5 * Sb, (got, conv, Sb)
+    rows = GOLD["eye"][(GOLD["eye"][:, 0] == 0) & np.isfinite(GOLD["eye"][:, 4])]
+    fld = R.fields.EarthDipole()
+    for mid, L, eqpa, Bm, ref, dip in rows:
+        tpos = np.array([0.0, L * Re, 0.0, 0.0])
+        assert abs(R.flutils.eye(tpos, fld, Bm) - ref) <= 2e-5 * ref
+        assert abs(R.flutils.eye(tpos, fld, Bm, usedipole=True) - dip) <= 1e-11 * dip
+    mid, x, y, z, Bm, gx, gy, gz = GOLD["gradI"][0]
+    g = R.flutils.gradI(np.array([0.0, x, y, z]), fld, Bm)
+    assert np.allclose(g, [gx, gy, gz], rtol=1e-3, atol=1e-3 * abs(gx))
