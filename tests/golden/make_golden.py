@@ -2,7 +2,7 @@
 """Generate tests/golden/golden.npz by running the unmodified RAPT reference.
 
 Run in a container that has the reference checked out (RAPT_REFERENCE_ROOT,
-default /root/reference); the GPU machine does not need it -- only the .npz travels.
+default /root/reference); the hosts that run the tests do not need it -- only the .npz travels.
 
 The reference is imported through oracle/shim.py. Per-call SciPy counters
 (NFCN, NSTEP, NACCPT, NREJCT = iwork[16:20]) are recorded by replacing the
