@@ -20,7 +20,10 @@ Contents:
          (the proton's last interval passes t = 8 s: the reference raises there)
   g3_*   one snapshot (time-independent), static True as the reference leaves it
   gout_* a proton that leaves the grid: the reference raises ValueError
+  ga*_   Adaptive protons switching between particle and guiding-centre modes
 """
+import contextlib
+import io
 import os
 import sys
 
@@ -160,6 +163,29 @@ def main():
     vel = proton_vel(f3, pos, 1e6, 90)
     out["gout_p_init"] = np.r_[pos, vel, m_pr, e]
     run(out, "gout_p", rapt.Particle(pos, vel, 0, m_pr, e, f3), 5.0, solvertolerances=(1e-8, 1e-8))
+    # ---- Adaptive in the five snapshots (static False) from t0 = 0.5 s: protons
+    # that start as particles and switch between the modes as they bounce
+    for case, (L, ke, pa) in (("ga0", (6.5, 1e6, 40.0)), ("ga1", (7.0, 2e6, 20.0))):
+        f4 = SynthGrid(GD.TIMES)
+        f4.static = False
+        pos = np.array([L * Re, 0.0, 0.0])
+        b = f4.unitb(np.r_[0.5, pos])
+        u = np.cross(b, [1.0, 0, 0])
+        u /= np.linalg.norm(u)
+        a = np.deg2rad(pa)
+        vel = rapt.utils.speedfromKE(ke, m_pr) * (np.cos(a) * b + np.sin(a) * u)
+        saved = dict(rapt.params)
+        rapt.params.update(solvertolerances=(1e-8, 1e-8), GCtimestep=0.5, cyclotronresolution=10)
+        ad = rapt.Adaptive(pos, vel, 0.5, m_pr, e, f4)
+        with contextlib.redirect_stdout(io.StringIO()):
+            ad.advance(3.0)  # Adaptive compares the absolute time with delta: ends at t = 3
+        rapt.params.clear()
+        rapt.params.update(saved)
+        out[case + "_init"] = np.r_[pos, vel, m_pr, e]
+        out[case + "_modes"] = np.array([0 if isinstance(s, rapt.Particle) else 1 for s in ad.trajlist])
+        out[case + "_t0s"] = np.array([s.trajectory[0, 0] for s in ad.trajlist])
+        last = ad.trajlist[-1].trajectory[-1]
+        out[case + "_final"] = np.r_[last, np.zeros(7 - len(last))]
     dst = os.path.join(HERE, "grid_golden.npz")
     np.savez_compressed(dst, **out)
     for k in sorted(out):

@@ -147,3 +147,22 @@ def test_facade_grid_parses_and_checks_bounds():
     assert not Tweaked(GD.TIMES).has_device_impl()
     with pytest.raises(AssertionError):  # fields.py:576
         F.Grid.__init__(type(g).__new__(type(g)), [])
+
+
+def test_grid_adaptive_matches_reference(oracle):
+    """Adaptive protons in the five-snapshot field (static False) that switch
+    between particle and guiding-centre modes: the switch sequence, the switch
+    times and the final state against the reference."""
+    f = grid4(oracle)
+    cfg = oracle.config(rtol=1e-8, atol=1e-8, gctimestep=0.5, cycres=10)
+    for case in ("ga0", "ga1"):
+        init = GOLD[case + "_init"]
+        tr = oracle.adaptive_init(f, cfg, init[0:3], init[3:6], 0.5, init[6], init[7])
+        modes = GOLD[case + "_modes"]
+        assert tr.mode == modes[0]
+        rc, rows, rmode, swt, swm = oracle.adaptive_advance(f, cfg, tr, 3.0)
+        assert tr.status == 0 and list(swm) == list(modes[1:]) and tr.mode == modes[-1], (case, list(swm))
+        assert np.allclose(swt, GOLD[case + "_t0s"][1:], rtol=1e-12, atol=0)
+        fin = GOLD[case + "_final"]
+        n = 7 if tr.mode == 0 else 5
+        assert np.allclose([tr.t, *tr.s[:n - 1]], fin[:n], rtol=1e-9), (case, [tr.t, *tr.s[:n - 1]], fin[:n])
