@@ -263,19 +263,25 @@ int rapt_bc_eval(void* ctx, int what, int64_t n, const double* tpos, const doubl
  * cudaMalloc -- applications that must not allocate once running (real-time
  * loops), libraries that own all device memory through their own pool, and code
  * that must not trigger the implicit device synchronisation an allocation or
- * free can cause. It advances up to RAPT_NOALLOC_MAX_TRACERS guiding centres
- * (GuidingCenter.advance, GuidingCenter.py:397-458, kind RAPT_KIND_GC) whose
- * state lives in caller-owned device memory, creates no context, and allocates
- * nothing: the work-queue heads, counters and per-tracer bookkeeping live in one
- * fixed __device__ array of RAPT_NOALLOC_SCRATCH_BYTES that every GPU loading
- * the library holds until the process exits.
+ * free can cause. It advances up to RAPT_NOALLOC_MAX_TRACERS guiding centres by
+ * delta (the same advance as rapt_advance with RAPT_KIND_GC) whose state lives
+ * in caller-owned device memory, creates no context, and allocates nothing:
+ * the work-queue heads, counters and per-tracer bookkeeping live in one fixed
+ * __device__ array of RAPT_NOALLOC_SCRATCH_BYTES that every GPU loading the
+ * library holds until the process exits.
  *  - n > RAPT_NOALLOC_MAX_TRACERS returns RAPT_ERR_INVALID and touches nothing.
- *  - The first call on a device looks up that array's address; make it before
- *    any stream capture on that device.
+ *  - It runs the plain FP64 form with a fixed cadence only: cfg->form other than
+ *    RAPT_FORM_PLAIN, cfg->gctimestep == 0 (the bounce-period cadence, which
+ *    needs field-line scratch), cfg->dense_output or cfg->collect returns
+ *    RAPT_ERR_UNSUPPORTED. rapt_config_default sets gctimestep = 0, so set it.
+ *  - The first call on a device looks up that array's address (again after the
+ *    device's context was reset); make it before any stream capture on that device.
  *  - All calls share the array: calls whose GPU work overlaps (other threads or
  *    streams on the same device) race and must be serialised by the caller.
+ *  - The call is synchronous: it returns after the GPU work has completed.
+ *    RAPT_ERR_STATE: tracers were still pending after 1,000,000 launch rounds.
  *  - nrows is reset to 0 by each call; rows[n][max_rows][7] receive the rows
- *    (t, x, y, z, ppar, 0, 0) of this call. Returns after the work completes. */
+ *    (t, x, y, z, ppar, 0, 0) of this call. */
 #define RAPT_NOALLOC_MAX_TRACERS 65536
 #define RAPT_NOALLOC_SCRATCH_BYTES 5242880
 typedef struct {

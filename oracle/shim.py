@@ -22,7 +22,9 @@ import types
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get("RAPT_REFERENCE_ROOT", "/root/reference")
+# The directory that holds the reference's ``rapt`` package; it must be named
+# by the environment (the hosts that run the tests do not have it).
+REFERENCE_ROOT = os.environ.get("RAPT_REFERENCE_ROOT", "")
 
 
 def _install_scipy_misc():
@@ -51,7 +53,8 @@ def load():
     if "rapt" in sys.modules and getattr(sys.modules["rapt"], "_graft_shimmed", False):
         return sys.modules["rapt"]
     if not os.path.isdir(os.path.join(REFERENCE_ROOT, "rapt")):
-        raise ImportError("RAPT reference not found at %s" % REFERENCE_ROOT)
+        raise ImportError("RAPT reference not found: set RAPT_REFERENCE_ROOT to the directory holding rapt/ "
+                          "(got %r)" % REFERENCE_ROOT)
     _install_scipy_misc()
     if REFERENCE_ROOT not in sys.path:
         sys.path.insert(0, REFERENCE_ROOT)

@@ -14,10 +14,19 @@
 // exits.
 //
 // The first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (with that device current); make that first call before
-// any stream capture. Every call reuses the same array and clears the parts that
-// must start at zero, so calls whose work overlaps on the GPU (two host threads,
-// or two streams, on the same device) race on it and must be serialised.
+// cudaGetSymbolAddress (with that device current) and keeps it, together with
+// the unique id of the device's context; a later call on a different context
+// (after cudaDeviceReset) looks the address up again. Make the first call on a
+// device before any stream capture on it. Every call reuses the same array and
+// clears the parts that must start at zero, so calls whose work overlaps on the
+// GPU (two host threads, or two streams, on the same device) race on it and
+// must be serialised. The call is synchronous: it returns after the GPU work
+// has completed.
+//
+// Only the configuration this path runs is accepted: the plain FP64 form, a
+// fixed output cadence (GCtimestep > 0), no dense output and no sample
+// collection; anything else returns RAPT_ERR_UNSUPPORTED rather than running
+// something other than what was asked.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -45,16 +54,52 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[RAPT_NOALLOC_SC
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_addr[kMaxDevices] = {nullptr};
+unsigned long long g_ctx_id[kMaxDevices] = {0};
 
-// Device address of g_noalloc_scratch on `device` (which must be current).
+// Unique id of the current CUDA context (cuCtxGetId, through the runtime's
+// driver entry points so that the library needs no link to libcuda), or 0 when
+// the driver does not provide it or no context is current.
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+unsigned long long current_ctx_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    looked_up = true;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", reinterpret_cast<void**>(&get_current), 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      get_current = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", reinterpret_cast<void**>(&get_id), 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      get_id = nullptr;
+    cudaGetLastError();
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, &id) == 0) return id;
+  return 0;
+}
+
+// Device address of g_noalloc_scratch on `device` (which must be current):
+// looked up once per device context. Without a context id (old driver) it is
+// looked up on every call.
 int scratch_address(int device, unsigned char** out) {
   if (device < 0 || device >= kMaxDevices) return RAPT_ERR_INVALID;
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[device]) {
+  const unsigned long long id = current_ctx_id();
+  if (!g_addr[device] || id == 0 || id != g_ctx_id[device]) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) return RAPT_ERR_CUDA;
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return RAPT_ERR_CUDA;
+    }
     g_addr[device] = p;
+    g_ctx_id[device] = current_ctx_id();  // the lookup may have created the context
   }
   *out = static_cast<unsigned char*>(g_addr[device]);
   return RAPT_OK;
@@ -144,6 +189,16 @@ extern "C" int rapt_gc_advance_noalloc(int device, int model, const double* para
   if (!std::isfinite(delta) || cfg->tableau < 0 || cfg->tableau > 1 || cfg->gc_eom < 0 || cfg->gc_eom > 2 ||
       cfg->nsteps <= 0 || st->max_rows < 2)
     return RAPT_ERR_INVALID;
+  // the range checks of rapt_config_set
+  if (!(cfg->rtol >= 0) || !(cfg->atol >= 0) || !(cfg->gctimestep >= 0) || !std::isfinite(cfg->gctimestep) ||
+      !(cfg->epss >= 0) || !(cfg->epst >= 0) || cfg->max_steps_per_launch < 0 ||
+      (cfg->tableau == 1 && !(cfg->rkf_tol > 0 && cfg->rkf_hmin >= 0)))
+    return RAPT_ERR_INVALID;
+  // what this path does not run: other forms, the bounce-period cadence
+  // (GCtimestep == 0 needs per-thread field-line scratch), dense output and
+  // sample collection
+  if (cfg->form != RAPT_FORM_PLAIN || cfg->gctimestep == 0.0 || cfg->dense_output || cfg->collect)
+    return RAPT_ERR_UNSUPPORTED;
   if (st->n == 0) return RAPT_OK;
   if (!st->t || !st->x || !st->y || !st->z || !st->ppar || !st->mu || !st->v || !st->mass || !st->charge ||
       !st->status || !st->naccept || !st->nreject || !st->nfcn || !st->rows || !st->row_mode || !st->nrows)
@@ -213,16 +268,17 @@ extern "C" int rapt_gc_advance_noalloc(int device, int model, const double* para
   if (cudaGetLastError() != cudaSuccess) return RAPT_ERR_CUDA;
   if (cudaMemsetAsync(S, 0, sizeof(Scratch), s) != cudaSuccess) return RAPT_ERR_CUDA;
   if (cudaMemsetAsync(st->nrows, 0, (size_t)E.n * sizeof(int32_t), s) != cudaSuccess) return RAPT_ERR_CUDA;
-  int64_t rounds = 0;
-  for (; rounds < 1000000; ++rounds) {
+  constexpr int64_t kMaxRounds = 1000000;
+  int64_t rounds = 0;  // guiding-centre kernel launches
+  unsigned long long pending = 1;
+  while (pending != 0 && rounds < kMaxRounds) {
     if (cudaMemsetAsync(S, 0, 3 * sizeof(unsigned long long), s) != cudaSuccess) return RAPT_ERR_CUDA;
     LaunchArgs a{E, P, S, sms * bps, block, s};
     if (T.gc[P.tableau](a) != cudaSuccess) return RAPT_ERR_CUDA;
-    unsigned long long pending = 0;
+    ++rounds;
     if (cudaMemcpyAsync(&pending, &S->pending, sizeof(pending), cudaMemcpyDeviceToHost, s) != cudaSuccess)
       return RAPT_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return RAPT_ERR_CUDA;
-    if (pending == 0) break;
   }
   if (stats) {
     Scratch hs;
@@ -234,8 +290,10 @@ extern "C" int rapt_gc_advance_noalloc(int device, int model, const double* para
     stats->rhs_evals = (int64_t)hs.rhs;
     stats->done = (int64_t)hs.done;
     stats->failed = (int64_t)hs.failed;
-    stats->launches = rounds + 1;
-    stats->kernel_launches = 2 * (rounds + 1);
+    stats->launches = rounds;
+    stats->kernel_launches = rounds + 1;  // the guiding-centre rounds and the one bookkeeping kernel
   }
+  // tracers still pending after the round cap: the advance did not finish
+  if (pending != 0) return RAPT_ERR_STATE;
   return RAPT_OK;
 }

@@ -3,8 +3,8 @@
 the second invariant (flutils.eye), its gradient (flutils.gradI), the dipole
 formula utils.dipoleI, and BounceCenter trajectories.
 
-Run where the reference is checked out (RAPT_REFERENCE_ROOT, default
-/root/reference); only the .npz travels. The reference is imported through
+Run where the reference is checked out, with RAPT_REFERENCE_ROOT naming that
+directory; only the .npz travels. The reference is imported through
 oracle/shim.py and used unmodified.
 
 Reference behaviour recorded here:

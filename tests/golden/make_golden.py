@@ -1,8 +1,8 @@
 #!/usr/bin/env python3
 """Generate tests/golden/golden.npz by running the unmodified RAPT reference.
 
-Run in a container that has the reference checked out (RAPT_REFERENCE_ROOT,
-default /root/reference); the hosts that run the tests do not need it -- only the .npz travels.
+Run where the reference is checked out, with RAPT_REFERENCE_ROOT naming that
+directory; the hosts that run the tests do not need it -- only the .npz travels.
 
 The reference is imported through oracle/shim.py. Per-call SciPy counters
 (NFCN, NSTEP, NACCPT, NREJCT = iwork[16:20]) are recorded by replacing the

@@ -1,8 +1,8 @@
 #!/usr/bin/env python3
 """Generate tests/golden/grid_golden.npz from the unmodified RAPT reference's Grid.
 
-Run where the reference is checked out (RAPT_REFERENCE_ROOT, default
-/root/reference); only the .npz travels. The snapshots come from grid_data.py
+Run where the reference is checked out, with RAPT_REFERENCE_ROOT naming that
+directory; only the .npz travels. The snapshots come from grid_data.py
 (computed, not stored). The reference's Grid is subclassed with a parsefile()
 that returns those snapshots by name -- the subclassing the reference asks for
 (fields.py:536-545) -- and is otherwise used as is.

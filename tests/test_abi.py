@@ -52,3 +52,32 @@ def test_no_gpu_fails_loudly_without_fallback():
         pytest.skip("a GPU is present")
     with pytest.raises(N.RaptError):
         N.Context(0)
+
+
+def test_noalloc_refuses_before_touching_the_device():
+    """The allocation-free entry point validates its configuration before any
+    CUDA call: the default configuration's bounce-period cadence, the FP32 and
+    learned forms, dense output, sample collection and bad tolerances are refused
+    with an error code (no GPU is needed to see that)."""
+    L = N.lib()
+    st = N.RaptGcDeviceState()
+    st.n = 16
+    st.max_rows = 4
+
+    def call(**over):
+        cfg = N.RaptConfig()
+        L.rapt_config_default(C.byref(cfg))
+        cfg.gctimestep = 1.0
+        for k, v in over.items():
+            setattr(cfg, k, v)
+        return L.rapt_gc_advance_noalloc(0, 1, None, 0, C.byref(cfg), C.byref(st), 1.0, None, None)
+
+    assert call(gctimestep=0.0) == N.RAPT_ERR_UNSUPPORTED
+    for form in (1, 2, 3):
+        assert call(form=form) == N.RAPT_ERR_UNSUPPORTED
+    assert call(dense_output=1) == N.RAPT_ERR_UNSUPPORTED
+    assert call(collect=1) == N.RAPT_ERR_UNSUPPORTED
+    assert call(rtol=-1.0) == N.RAPT_ERR_INVALID
+    assert call(gctimestep=-1.0) == N.RAPT_ERR_INVALID
+    st.n = N.NOALLOC_MAX_TRACERS + 1
+    assert call() == N.RAPT_ERR_INVALID

@@ -63,7 +63,7 @@ def test_noalloc_matches_context_path_twice():
     for call in range(2):
         ref_stats = ens.advance("gc", 1.0)
         ref = ens.download()
-        rows, _, nrows, _, _ = ens.rows(reset=True)
+        rows, row_mode, nrows, _, _ = ens.rows(reset=True)
         stats = N.RaptStats()
         rc = N.lib().rapt_gc_advance_noalloc(0, ens.field.model_id, params.ctypes.data_as(N._DP), len(params),
                                              C.byref(cfg), C.byref(st), 1.0, stream, C.byref(stats))
@@ -76,9 +76,31 @@ def test_noalloc_matches_context_path_twice():
         assert np.array_equal(got["status"], ref["status"])
         for k in ("naccept", "nreject", "nfcn"):
             assert np.array_equal(got[k], ref[k]), (call, k)
-        assert np.array_equal(got["nrows"], nrows)
-        np.testing.assert_allclose(got["rows"][:, :1], rows[:, :1], rtol=1e-12, atol=0)
+        assert np.array_equal(got["nrows"], nrows) and nrows.min() >= 1
+        # every row this call produced (the end-of-interval rows included) and its mode
+        for k in range(n):
+            m = nrows[k]
+            np.testing.assert_allclose(got["rows"][k, :m], rows[k, :m], rtol=1e-12, atol=1e-300,
+                                       err_msg="call %d tracer %d" % (call, k))
+            assert np.array_equal(got["row_mode"][k, :m], row_mode[k, :m]), (call, k)
         assert stats.accepted == ref_stats["accepted"] > 0
+
+
+def test_noalloc_rejects_what_it_does_not_run():
+    """The default configuration has GCtimestep = 0 (bounce-period cadence), which
+    this path does not run: the call must refuse it, not report success with
+    every tracer unadvanced. The same for the other forms."""
+    st = N.RaptGcDeviceState()
+    st.n = 16
+    st.max_rows = MAX_ROWS
+    cfg = N.RaptConfig()
+    N.lib().rapt_config_default(C.byref(cfg))
+    rc = N.lib().rapt_gc_advance_noalloc(0, 1, None, 0, C.byref(cfg), C.byref(st), 1.0, None, None)
+    assert rc == N.RAPT_ERR_UNSUPPORTED
+    cfg.gctimestep = 1.0
+    cfg.form = 1
+    rc = N.lib().rapt_gc_advance_noalloc(0, 1, None, 0, C.byref(cfg), C.byref(st), 1.0, None, None)
+    assert rc == N.RAPT_ERR_UNSUPPORTED
 
 
 def test_noalloc_rejects_too_many_tracers():
