@@ -687,14 +687,19 @@ int dop853(F& f, int n, double& x, double* y, double xend, double rtol, double a
 template <class F>
 int rkf45(F& f, int n, double& t, double* x, double b, double tol, double hmax, double hmin,
           Counters& cnt, int max_iter) {
-  const double a2 = 2.5e-01, a3 = 3.75e-01, a4 = 12.0 / 13.0, a5 = 1.0, a6 = 0.5;
-  const double b21 = 0.25, b31 = 3.0 / 32.0, b32 = 9.0 / 32.0, b41 = 1932.0 / 2197.0,
-               b42 = -7200.0 / 2197.0, b43 = 7296.0 / 2197.0, b51 = 439.0 / 216.0, b52 = -8.0,
-               b53 = 3680.0 / 513.0, b54 = -845.0 / 4104.0, b61 = -8.0 / 27.0, b62 = 2.0,
-               b63 = -3544.0 / 2565.0, b64 = 1859.0 / 4104.0, b65 = -11.0 / 40.0;
-  const double r1 = 1.0 / 360.0, r3 = -128.0 / 4275.0, r4 = -2197.0 / 75240.0, r5 = 1.0 / 50.0,
-               r6 = 2.0 / 55.0;
-  const double c1 = 25.0 / 216.0, c3 = 1408.0 / 2565.0, c4 = 2197.0 / 4104.0, c5 = -1.0 / 5.0;
+  // the decimal coefficients of rkf.py:48-87 (several differ from the exact
+  // fractions in the last bit)
+  const double a2 = 2.500000000000000e-01, a3 = 3.750000000000000e-01, a4 = 9.230769230769231e-01, a5 = 1.0,
+               a6 = 5.000000000000000e-01;
+  const double b21 = 2.500000000000000e-01, b31 = 9.375000000000000e-02, b32 = 2.812500000000000e-01,
+               b41 = 8.793809740555303e-01, b42 = -3.277196176604461e+00, b43 = 3.320892125625853e+00,
+               b51 = 2.032407407407407e+00, b52 = -8.000000000000000e+00, b53 = 7.173489278752436e+00,
+               b54 = -2.058966861598441e-01, b61 = -2.962962962962963e-01, b62 = 2.000000000000000e+00,
+               b63 = -1.381676413255361e+00, b64 = 4.529727095516569e-01, b65 = -2.750000000000000e-01;
+  const double r1 = 2.777777777777778e-03, r3 = -2.994152046783626e-02, r4 = -2.919989367357789e-02,
+               r5 = 2.000000000000000e-02, r6 = 3.636363636363636e-02;
+  const double c1 = 1.157407407407407e-01, c3 = 5.489278752436647e-01, c4 = 5.353313840155945e-01,
+               c5 = -2.000000000000000e-01;
   double h = hmax;
   double k1[6], k2[6], k3[6], k4[6], k5[6], k6[6], xt[6];
   int it = 0;
@@ -1016,8 +1021,10 @@ int orc_particle_advance(const orc_field* f, const orc_config* c, orc_tracer* p,
     const int method = (c->tableau == 1) ? 2 : 0;
     const int idid = orc_integrate_particle(f, c, method, p->mass, p->charge, gm, &rt, y, rt + dt, 0.1, cnt);
     p->nfcn += cnt[0]; p->nstep += cnt[1]; p->naccept += cnt[2]; p->nreject += cnt[3];
-    if (idid == -6) {  // Grid: the reference raises ValueError inside r.integrate(): no row, state kept
-      p->status = ORC_ST_OUT_OF_GRID;
+    if (idid == -6 || idid == -5) {
+      // Grid: the reference raises ValueError inside r.integrate(); RKF45: rkf.py
+      // raises RuntimeError at hmin (rkf.py:136-139). No row, state kept.
+      p->status = idid == -6 ? ORC_ST_OUT_OF_GRID : ORC_ST_RKF_HMIN;
       break;
     }
     if (idid < 0) {
@@ -1179,8 +1186,10 @@ int orc_gc_advance(const orc_field* f, const orc_config* c, orc_tracer* g, doubl
     const int method = (c->tableau == 1) ? 2 : 1;
     const int idid = orc_integrate_gc(f, c, method, g->mass, g->charge, g->mu, g->v, &rt, y, rt + dt, cnt);
     g->nfcn += cnt[0]; g->nstep += cnt[1]; g->naccept += cnt[2]; g->nreject += cnt[3];
-    if (idid == -6) {  // Grid: the reference raises ValueError inside r.integrate(): no row, state kept
-      g->status = ORC_ST_OUT_OF_GRID;
+    if (idid == -6 || idid == -5) {
+      // Grid: the reference raises ValueError inside r.integrate(); RKF45: rkf.py
+      // raises RuntimeError at hmin (rkf.py:136-139). No row, state kept.
+      g->status = idid == -6 ? ORC_ST_OUT_OF_GRID : ORC_ST_RKF_HMIN;
       break;
     }
     if (idid < 0) {

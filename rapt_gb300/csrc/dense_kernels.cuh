@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(128) k_gc_dense(DevEnsemble E, KParams P, Scra
     if (!(seg_ok && t_row < stop)) {
       bool more = false;
       if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_BAD_INPUT &&
-          status != RAPT_ST_OUT_OF_GRID && tcur < delta) {
+          status != RAPT_ST_OUT_OF_GRID && status != RAPT_ST_RKF_HMIN && tcur < delta) {
         if (nseg + 1 >= P.max_segments) {
           status = RAPT_ST_ADAPTIVE_LIMIT;
         } else {

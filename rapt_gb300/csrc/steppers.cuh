@@ -281,20 +281,26 @@ __device__ __forceinline__ void dop853_attempt(const F& f, double x, const doubl
   err = fabs(h) * e5 * sqrt(1.0 / (NV * deno));
 }
 
-// One RKF45 attempt as restated from rapt/rkf.py:101-124: k_i = h f(...),
+// One RKF45 attempt as restated from rapt/rkf.py:101-124 (coefficients
+// rkf.py:48-87): k_i = h f(...),
 // error r = max_i |sum r_j k_j| / h, 4th-order solution y1. NANPROP: r is NaN
 // when any term is (a Grid stage outside the grid), which fmax alone would drop.
 template <int NV, bool NANPROP = false, class F>
 __device__ __forceinline__ void rkf45_attempt(const F& f, double t, const double* x, double h, double* y1,
                                               double& r) {
-  constexpr double a2 = 0.25, a3 = 0.375, a4 = 12.0 / 13.0, a5 = 1.0, a6 = 0.5;
-  constexpr double b21 = 0.25, b31 = 3.0 / 32.0, b32 = 9.0 / 32.0, b41 = 1932.0 / 2197.0,
-                   b42 = -7200.0 / 2197.0, b43 = 7296.0 / 2197.0, b51 = 439.0 / 216.0, b52 = -8.0,
-                   b53 = 3680.0 / 513.0, b54 = -845.0 / 4104.0, b61 = -8.0 / 27.0, b62 = 2.0,
-                   b63 = -3544.0 / 2565.0, b64 = 1859.0 / 4104.0, b65 = -11.0 / 40.0;
-  constexpr double r1 = 1.0 / 360.0, r3 = -128.0 / 4275.0, r4 = -2197.0 / 75240.0, r5 = 1.0 / 50.0,
-                   r6 = 2.0 / 55.0;
-  constexpr double c1 = 25.0 / 216.0, c3 = 1408.0 / 2565.0, c4 = 2197.0 / 4104.0, c5 = -1.0 / 5.0;
+  // the decimal coefficients of rkf.py:48-87 (several differ from the exact
+  // fractions in the last bit)
+  constexpr double a2 = 2.500000000000000e-01, a3 = 3.750000000000000e-01, a4 = 9.230769230769231e-01, a5 = 1.0,
+                   a6 = 5.000000000000000e-01;
+  constexpr double b21 = 2.500000000000000e-01, b31 = 9.375000000000000e-02, b32 = 2.812500000000000e-01,
+                   b41 = 8.793809740555303e-01, b42 = -3.277196176604461e+00, b43 = 3.320892125625853e+00,
+                   b51 = 2.032407407407407e+00, b52 = -8.000000000000000e+00, b53 = 7.173489278752436e+00,
+                   b54 = -2.058966861598441e-01, b61 = -2.962962962962963e-01, b62 = 2.000000000000000e+00,
+                   b63 = -1.381676413255361e+00, b64 = 4.529727095516569e-01, b65 = -2.750000000000000e-01;
+  constexpr double r1 = 2.777777777777778e-03, r3 = -2.994152046783626e-02, r4 = -2.919989367357789e-02,
+                   r5 = 2.000000000000000e-02, r6 = 3.636363636363636e-02;
+  constexpr double c1 = 1.157407407407407e-01, c3 = 5.489278752436647e-01, c4 = 5.353313840155945e-01,
+                   c5 = -2.000000000000000e-01;
   double k1[NV], k2[NV], k3[NV], k4[NV], k5[NV], k6[NV], xt[NV];
   f(t, x, k1);
 #pragma unroll

@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(128) k_particle(DevEnsemble E, KParams P, Scra
       if (!(seg_ok && rt < stop)) {
         // end of this Particle.advance() call
         bool more = false;
-        if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_OUT_OF_GRID &&
+        if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_OUT_OF_GRID && status != RAPT_ST_RKF_HMIN &&
             tcur < delta) {
           if (nseg + 1 >= P.max_segments) {
             status = RAPT_ST_ADAPTIVE_LIMIT;
@@ -473,8 +473,9 @@ __global__ void __launch_bounds__(128) k_particle(DevEnsemble E, KParams P, Scra
       in_interval = false;
       if (fail) { seg_ok = false; status = fail; }
       if (!all_finite<6>(y)) { seg_ok = false; status = RAPT_ST_NONFINITE; }
-      // a Grid step outside the grid: the reference raises inside the interval, adding no row
-      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID);
+      // a Grid step outside the grid (ValueError) or an RKF45 step below hmin
+      // (RuntimeError): the reference raises inside the interval, adding no row
+      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID) && status != RAPT_ST_RKF_HMIN;
       if (row) {
         t_row = rowt;
         tcur = rt + dt;  // Particle.py:306
@@ -622,7 +623,7 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
       if (!(seg_ok && rt < stop)) {
         bool more = false;
         if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_BAD_INPUT &&
-            status != RAPT_ST_OUT_OF_GRID && tcur < delta) {
+            status != RAPT_ST_OUT_OF_GRID && status != RAPT_ST_RKF_HMIN && tcur < delta) {
           if (nseg + 1 >= P.max_segments) {
             status = RAPT_ST_ADAPTIVE_LIMIT;
           } else {
@@ -766,8 +767,9 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
       in_interval = false;
       if (fail) { seg_ok = false; status = fail; }
       if (!all_finite<4>(y)) { seg_ok = false; status = RAPT_ST_NONFINITE; }
-      // a Grid step outside the grid: the reference raises inside the interval, adding no row
-      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID);
+      // a Grid step outside the grid (ValueError) or an RKF45 step below hmin
+      // (RuntimeError): the reference raises inside the interval, adding no row
+      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID) && status != RAPT_ST_RKF_HMIN;
       if (row) {
         t_row = rt;
         tcur = rt;

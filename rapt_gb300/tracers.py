@@ -552,9 +552,13 @@ def _advance_bc(tracers, delta):
 
 def _raise_if_left_grid(res):
     # a Grid field evaluated outside its grid: the reference's interpolator raises
-    # ValueError from inside the step (fields.py:733-737); the rows before it stay
+    # ValueError from inside the step (fields.py:733-737); the RKF45 tableau below
+    # its minimum step: rkf.py raises RuntimeError (rkf.py:136-139). The rows
+    # before the failing interval stay.
     if res["status"] is not None and res["status"][0] == N.ST["OUT_OF_GRID"]:
         raise ValueError("One of the requested xi is out of bounds: the tracer left the Grid field's grid")
+    if res["status"] is not None and res["status"][0] == N.ST["RKF_HMIN"]:
+        raise RuntimeError("Error: Could not converge to the required tolerance with minimum stepsize (RKF45)")
 
 
 def advance_batch(tracers, delta, eom="TaoChanBrizardEOM", tableau=0, verbose=False):
