@@ -333,8 +333,15 @@ int rapt_mlp_samples_reserve(void* ctx, int64_t capacity, uint64_t mask);
 int rapt_mlp_samples_count(void* ctx, int64_t* count);
 int rapt_mlp_samples_download(void* ctx, float* out, int64_t first, int64_t n);
 int rapt_mlp_samples_upload(void* ctx, const float* samples, int64_t n);
+/* Put samples [first, first + n) into a canonical order (sorted by a 64-bit
+ * hash of each sample's words). The kernels append samples in an order set by
+ * device atomics; after this call the order, and so the minibatches that
+ * rapt_mlp_train draws, depend only on which samples were collected. */
+int rapt_mlp_samples_sort(void* ctx, int64_t first, int64_t n);
 /* Adam (0.9, 0.999, 1e-8) on minibatches drawn from the device samples;
- * loss[2] = mean (step, switch) loss over the last tenth of the steps. */
+ * loss[2] = mean (step, switch) loss over the last tenth of the steps.
+ * Deterministic: gradients are reduced in a fixed order (no floating-point
+ * atomics), so equal samples, seed and parameters give equal results. */
 int rapt_mlp_train(void* ctx, int64_t steps, int32_t batch, float lr, float switch_weight, uint64_t seed,
                    double* loss);
 

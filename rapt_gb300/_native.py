@@ -94,6 +94,7 @@ SIGNATURES = {
     "rapt_mlp_samples_count": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
     "rapt_mlp_samples_download": (C.c_int, [_VP, _VP, _I64, _I64]),
     "rapt_mlp_samples_upload": (C.c_int, [_VP, _VP, _I64]),
+    "rapt_mlp_samples_sort": (C.c_int, [_VP, _I64, _I64]),
     "rapt_mlp_train": (C.c_int, [_VP, _I64, C.c_int32, C.c_float, C.c_float, C.c_uint64, _DP]),
 }
 
@@ -303,6 +304,12 @@ class Context:
     def mlp_samples_upload(self, samples):
         s = np.ascontiguousarray(samples, dtype=np.float32).reshape(-1, MLP_SAMPLE)
         self.check(self.L.rapt_mlp_samples_upload(self.h, ptr(s), s.shape[0]), "rapt_mlp_samples_upload")
+
+    def mlp_samples_sort(self, first=0, n=None):
+        """Canonical order of samples [first, first + n) (rapt_mlp_samples_sort)."""
+        if n is None:
+            n = self.mlp_samples_count() - first
+        self.check(self.L.rapt_mlp_samples_sort(self.h, int(first), int(n)), "rapt_mlp_samples_sort")
 
     def mlp_train(self, steps, batch=4096, lr=1e-3, switch_weight=1.0, seed=0):
         loss = (C.c_double * 2)()

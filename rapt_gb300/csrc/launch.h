@@ -59,9 +59,18 @@ struct ModelTable {
 constexpr int kMlpPackedWords = 64 * 8 + 64 * 32 + 8 * 32 + 64 * 32 + 64 * 4 + 8 * 32 * 2 + 8 * 32 * 8 + 32 * 8 +
                                  32 * 16 + 32 * 16 + 32 * 2;
 cudaError_t mlp_pack(const float* p, uint32_t* w, cudaStream_t s);
+// training gradient: at most kMlpTrainMaxBlocks blocks, each writing a partial
+// gradient of kMlpGaccWords floats and two loss doubles to the workspaces
+constexpr int kMlpTrainMaxBlocks = 1024;
+constexpr int kMlpGaccWords = (RAPT_MLP_NTRAIN + 31) / 32 * 32;
 cudaError_t mlp_grad(const float* samples, int64_t nsamp, int64_t batch, int random, uint64_t seed, int64_t step,
-                     float switch_weight, const uint32_t* w, const float* p, float* grad, double* loss, int num_sms,
-                     cudaStream_t s);
+                     float switch_weight, const uint32_t* w, const float* p, float* grad, double* loss, float* partial,
+                     double* lpart, cudaStream_t s);
+// canonical order of n samples (a 64-bit hash of each sample's words, sorted):
+// the kernels append samples in an order set by atomics; after this the order
+// depends only on the set of samples. tmp: mlp_sort_tmp_bytes(n) bytes.
+size_t mlp_sort_tmp_bytes(int64_t n);
+cudaError_t mlp_samples_sort(float* samples, int64_t n, void* tmp, size_t tmp_bytes, cudaStream_t s);
 cudaError_t mlp_adam(float* p, float* m, float* v, const float* g, float lr, int64_t t, cudaStream_t s);
 cudaError_t mlp_forward(const uint32_t* w, const float* p, const float* feat, int64_t n, float* out, int num_sms,
                         cudaStream_t s);

@@ -6,8 +6,13 @@
 // (label >= 0); the batch loss is the mean. Backward pass per 32-sample chunk (one warp):
 //   dO -> dW3, db3 (CUDA cores), dZ2 = (dO W3^T) * [H2 > 0] (BF16),
 //   dW2 = H1^T dZ2, dH1 = dZ2 W2^T, dZ1 = dH1 * [H1 > 0], dW1 = X^T dZ1
-// (mma.sync), with the chunk's weight gradients summed in shared memory and
-// one global atomicAdd per parameter per block.
+// (mma.sync). Deterministic: one warp per block sums its chunks' weight
+// gradients in shared memory in program order (each lane adds to its own
+// addresses), writes the block's partial gradient, and k_mlp_reduce sums the
+// partials over the blocks in a fixed order -- no floating-point atomics, so
+// the same samples, seed and parameters give the same bits on every run.
+#include <cub/device/device_radix_sort.cuh>
+
 #include "mlp.cuh"
 #include "launch.h"
 
@@ -15,7 +20,8 @@ namespace rapt {
 namespace {
 
 static_assert(kMlpPacked == kMlpPackedWords, "packed weight size");
-constexpr int kTrainWarps = 4;
+static_assert(((kMlpTrainable + 31) / 32 * 32) == kMlpGaccWords, "partial gradient stride");
+constexpr int kTrainWarps = 1;  // one warp per block: see the header
 // per-warp shared memory (u32): X, XT, H1, H1T, H2, dZ2, dZ2T, dZ1T, dO
 constexpr int kSX = 0, kSXT = 256, kSH1 = 512, kSH1T = 1536, kSH2 = 2560, kSDZ2 = 3584, kSDZ2T = 4608,
               kSDZ1T = 5632, kSDO = 6656, kWarpSmemTrain = 6720;
@@ -32,8 +38,8 @@ struct TrainArgs {
   float inv_batch, switch_weight;
   const uint32_t* w;
   const float* p;
-  float* grad;           // [kMlpTrainable], accumulated
-  double* loss;          // [2]: step loss sum, switch loss sum (divided by batch)
+  float* partial;        // [gridDim.x][kGaccWords] per-block gradient sums
+  double* lpart;         // [gridDim.x][2] per-block (step, switch) loss sums (divided by batch)
 };
 
 __device__ __forceinline__ void st16(uint32_t* base, int idx16, uint32_t v16) {
@@ -115,17 +121,17 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_mlp_train(TrainArgs a) {
         const float h0 = bf16_lo(u), h1 = bf16_hi(u), e0 = DO[2 * s], e1 = DO[2 * s + 1];
         a00 += h0 * e0; a01 += h0 * e1; a10 += h1 * e0; a11 += h1 * e1;
       }
-      atomicAdd(&gacc[kOffW3 + 2 * lane], a00);
-      atomicAdd(&gacc[kOffW3 + 64 + 2 * lane], a01);
-      atomicAdd(&gacc[kOffW3 + 2 * lane + 1], a10);
-      atomicAdd(&gacc[kOffW3 + 64 + 2 * lane + 1], a11);
+      gacc[kOffW3 + 2 * lane] += a00;
+      gacc[kOffW3 + 64 + 2 * lane] += a01;
+      gacc[kOffW3 + 2 * lane + 1] += a10;
+      gacc[kOffW3 + 64 + 2 * lane + 1] += a11;
       float s0 = d0, s1 = d1;
 #pragma unroll
       for (int m = 16; m > 0; m >>= 1) {
         s0 += __shfl_xor_sync(kFull, s0, m);
         s1 += __shfl_xor_sync(kFull, s1, m);
       }
-      if (lane == 0) { atomicAdd(&gacc[kOffB3], s0); atomicAdd(&gacc[kOffB3 + 1], s1); }
+      if (lane == 0) { gacc[kOffB3] += s0; gacc[kOffB3 + 1] += s1; }
     }
     // ---- dZ2 = (dO W3^T) * [H2 > 0], lane = sample
     {
@@ -154,8 +160,8 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_mlp_train(TrainArgs a) {
         s0 += bf16_lo(u0) + bf16_hi(u0);
         s1 += bf16_lo(u1) + bf16_hi(u1);
       }
-      atomicAdd(&gacc[kOffB2 + 2 * lane], s0);
-      atomicAdd(&gacc[kOffB2 + 2 * lane + 1], s1);
+      gacc[kOffB2 + 2 * lane] += s0;
+      gacc[kOffB2 + 2 * lane + 1] += s1;
     }
     // ---- dW2[in m][out n] = sum_s H1[s][m] dZ2[s][n]; stored as W2T[n][m]
 #pragma unroll 1
@@ -171,10 +177,10 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_mlp_train(TrainArgs a) {
           mma_bf16(cc, af, bf);
         }
         const int m0 = 16 * t + g, n0 = 8 * j + 2 * q;
-        atomicAdd(&gacc[kOffW2 + n0 * 64 + m0], cc[0]);
-        atomicAdd(&gacc[kOffW2 + (n0 + 1) * 64 + m0], cc[1]);
-        atomicAdd(&gacc[kOffW2 + n0 * 64 + m0 + 8], cc[2]);
-        atomicAdd(&gacc[kOffW2 + (n0 + 1) * 64 + m0 + 8], cc[3]);
+        gacc[kOffW2 + n0 * 64 + m0] += cc[0];
+        gacc[kOffW2 + (n0 + 1) * 64 + m0] += cc[1];
+        gacc[kOffW2 + n0 * 64 + m0 + 8] += cc[2];
+        gacc[kOffW2 + (n0 + 1) * 64 + m0 + 8] += cc[3];
       }
     }
     // ---- dZ1 = (dZ2 W2^T) * [H1 > 0] -> dZ1T [64 in][32 samples]
@@ -211,8 +217,8 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_mlp_train(TrainArgs a) {
         s0 += bf16_lo(u0) + bf16_hi(u0);
         s1 += bf16_lo(u1) + bf16_hi(u1);
       }
-      atomicAdd(&gacc[kOffB1 + 2 * lane], s0);
-      atomicAdd(&gacc[kOffB1 + 2 * lane + 1], s1);
+      gacc[kOffB1 + 2 * lane] += s0;
+      gacc[kOffB1 + 2 * lane + 1] += s1;
     }
     // ---- dW1[in m][out n] = sum_s X[s][m] dZ1[s][n]; stored as W1T[n][m]
 #pragma unroll 2
@@ -226,27 +232,42 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_mlp_train(TrainArgs a) {
         mma_bf16(cc, af, bf);
       }
       const int n0 = 8 * j + 2 * q;
-      atomicAdd(&gacc[kOffW1 + n0 * 16 + g], cc[0]);
-      atomicAdd(&gacc[kOffW1 + (n0 + 1) * 16 + g], cc[1]);
-      atomicAdd(&gacc[kOffW1 + n0 * 16 + g + 8], cc[2]);
-      atomicAdd(&gacc[kOffW1 + (n0 + 1) * 16 + g + 8], cc[3]);
+      gacc[kOffW1 + n0 * 16 + g] += cc[0];
+      gacc[kOffW1 + (n0 + 1) * 16 + g] += cc[1];
+      gacc[kOffW1 + n0 * 16 + g + 8] += cc[2];
+      gacc[kOffW1 + (n0 + 1) * 16 + g + 8] += cc[3];
     }
     __syncwarp();
   }
-  // loss: warp reduce, one atomic per warp
+  // loss: warp reduce (a fixed butterfly order)
 #pragma unroll
   for (int m = 16; m > 0; m >>= 1) {
     l0sum += __shfl_xor_sync(kFull, l0sum, m);
     l1sum += __shfl_xor_sync(kFull, l1sum, m);
   }
   if (lane == 0) {
-    atomicAdd(&a.loss[0], l0sum * (double)a.inv_batch);
-    atomicAdd(&a.loss[1], l1sum * (double)a.inv_batch);
+    a.lpart[2 * blockIdx.x] = l0sum * (double)a.inv_batch;
+    a.lpart[2 * blockIdx.x + 1] = l1sum * (double)a.inv_batch;
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < kMlpTrainable; i += blockDim.x) {
-    const float v = gacc[i];
-    if (v != 0.f) atomicAdd(&a.grad[i], v);
+  __syncwarp();
+  float* dst = a.partial + (size_t)blockIdx.x * kGaccWords;
+  for (int i = threadIdx.x; i < kGaccWords; i += blockDim.x) dst[i] = gacc[i];
+}
+
+// grad[i] = sum over blocks of partial[b][i], blocks in order; thread 0 of
+// block 0 adds the loss partials to loss[0..1] in order.
+__global__ void k_mlp_reduce(const float* partial, const double* lpart, int nblocks, float* grad, double* loss) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kMlpTrainable) {
+    float s = 0.f;
+    for (int b = 0; b < nblocks; ++b) s += partial[(size_t)b * kGaccWords + i];
+    grad[i] = s;
+  }
+  if (i == 0 && loss) {
+    double l0 = 0, l1 = 0;
+    for (int b = 0; b < nblocks; ++b) { l0 += lpart[2 * b]; l1 += lpart[2 * b + 1]; }
+    loss[0] += l0;
+    loss[1] += l1;
   }
 }
 
@@ -330,7 +351,65 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const uint32_t* w, const fl
   }
 }
 
+// Sort key of a sample: a 64-bit hash of its 18 words (mix64 chained over the
+// words); the value is the sample's index.
+__global__ void k_sample_keys(const float* samples, int64_t n, unsigned long long* keys, uint32_t* idx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t* w = reinterpret_cast<const uint32_t*>(samples + i * kSampleStride);
+  uint64_t h = 0x243f6a8885a308d3ull;
+#pragma unroll
+  for (int k = 0; k < kSampleStride; ++k) h = mix64(h ^ w[k]);
+  keys[i] = h;
+  idx[i] = (uint32_t)i;
+}
+
+__global__ void k_sample_gather(const float* src, const uint32_t* idx, int64_t n, float* dst) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * kSampleStride) return;
+  const int64_t i = t / kSampleStride, k = t % kSampleStride;
+  dst[t] = src[(int64_t)idx[i] * kSampleStride + k];
+}
+
 }  // namespace
+
+// Workspace of mlp_samples_sort: keys in/out, indices in/out, the gathered
+// copy, and CUB's radix-sort storage, each 256-byte aligned.
+static size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+static size_t cub_sort_bytes(int64_t n) {
+  size_t b = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, b, (const unsigned long long*)nullptr, (unsigned long long*)nullptr,
+                                  (const uint32_t*)nullptr, (uint32_t*)nullptr, (int)n);
+  return b;
+}
+size_t mlp_sort_tmp_bytes(int64_t n) {
+  return 2 * al256((size_t)n * 8) + 2 * al256((size_t)n * 4) + al256((size_t)n * kSampleStride * 4) +
+         al256(cub_sort_bytes(n));
+}
+
+cudaError_t mlp_samples_sort(float* samples, int64_t n, void* tmp, size_t tmp_bytes, cudaStream_t s) {
+  if (n <= 1) return cudaSuccess;
+  if (n > 0x7fffffffLL || tmp_bytes < mlp_sort_tmp_bytes(n)) return cudaErrorInvalidValue;
+  char* p = static_cast<char*>(tmp);
+  auto take = [&](size_t b) { char* q = p; p += al256(b); return q; };
+  auto* k0 = reinterpret_cast<unsigned long long*>(take((size_t)n * 8));
+  auto* k1 = reinterpret_cast<unsigned long long*>(take((size_t)n * 8));
+  auto* i0 = reinterpret_cast<uint32_t*>(take((size_t)n * 4));
+  auto* i1 = reinterpret_cast<uint32_t*>(take((size_t)n * 4));
+  auto* copy = reinterpret_cast<float*>(take((size_t)n * kSampleStride * 4));
+  size_t cb = cub_sort_bytes(n);
+  void* cubtmp = take(cb);
+  k_sample_keys<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(samples, n, k0, i0);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = cub::DeviceRadixSort::SortPairs(cubtmp, cb, k0, k1, i0, i1, (int)n, 0, 64, s);
+  if (e != cudaSuccess) return e;
+  const int64_t words = n * kSampleStride;
+  k_sample_gather<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(samples, i1, n, copy);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(samples, copy, (size_t)words * 4, cudaMemcpyDeviceToDevice, s);
+}
 
 cudaError_t mlp_pack(const float* p, uint32_t* w, cudaStream_t s) {
   k_mlp_pack<<<(kMlpPacked + 255) / 256, 256, 0, s>>>(p, w);
@@ -338,20 +417,23 @@ cudaError_t mlp_pack(const float* p, uint32_t* w, cudaStream_t s) {
 }
 
 cudaError_t mlp_grad(const float* samples, int64_t nsamp, int64_t batch, int random, uint64_t seed, int64_t step,
-                     float switch_weight, const uint32_t* w, const float* p, float* grad, double* loss, int num_sms,
-                     cudaStream_t s) {
+                     float switch_weight, const uint32_t* w, const float* p, float* grad, double* loss, float* partial,
+                     double* lpart, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmemBytes);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  TrainArgs a{samples, nsamp, batch, random, seed, step, 1.f / (float)batch, switch_weight, w, p, grad, loss};
+  TrainArgs a{samples, nsamp, batch, random, seed, step, 1.f / (float)batch, switch_weight, w, p, partial, lpart};
   const int64_t chunks = (batch + 31) / 32;
-  int64_t grid = (chunks + 2 * kTrainWarps - 1) / (2 * kTrainWarps);  // two chunks per warp
-  if (grid > 2 * num_sms) grid = 2 * num_sms;
+  int64_t grid = (chunks + 1) / 2;  // two chunks per warp
+  if (grid > kMlpTrainMaxBlocks) grid = kMlpTrainMaxBlocks;
   if (grid < 1) grid = 1;
   k_mlp_train<<<(unsigned)grid, kTrainWarps * 32, kTrainSmemBytes, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_mlp_reduce<<<(kMlpTrainable + 255) / 256, 256, 0, s>>>(partial, lpart, (int)grid, grad, loss);
   return cudaGetLastError();
 }
 

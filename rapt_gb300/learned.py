@@ -103,6 +103,7 @@ def collect_gc(workload, seconds, capacity=1 << 21, mask=0, ctx=None, form=0):
     ens.configure(collect=1)
     st = ens.advance("gc", float(seconds))
     ens.configure(collect=0)
+    ctx.mlp_samples_sort()
     return ens, st, ctx.mlp_samples_count()
 
 
@@ -148,6 +149,7 @@ def fit_gc(workload, seconds, ctx=None, rounds=2, steps=3000, batch=4096, lr=2e-
                                      learned_scale=scale)
         st = ens.advance("gc", float(seconds))
         n1 = ctx.mlp_samples_count()
+        ctx.mlp_samples_sort(n0, n1 - n0)  # canonical order: training is then reproducible
         info["collect"].append({"form": form, "accepted": st["accepted"], "rejected": st["rejected"],
                                 "samples": n1 - n0})
         return n0, n1
@@ -167,6 +169,48 @@ def fit_gc(workload, seconds, ctx=None, rounds=2, steps=3000, batch=4096, lr=2e-
         info["calibration"].append(cal)
     info["scale"] = cal["scale"]
     return p, info
+
+
+def calibrate_global(workload, seconds, ctx=None, scales=(1.0, 0.95, 0.9, 0.85, 0.8, 0.75, 0.7, 0.65, 0.6),
+                     form=3, every=1, quantile=0.99):
+    """Proposal scale calibrated on the global error, with the network loaded in
+    ctx: guiding centres of `workload` are advanced `seconds` by the plain FP64
+    controller, by a tight-tolerance run (rtol = atol = 1e-12, the exact
+    solution) and by the learned form at each candidate scale, largest first.
+    The chosen scale is the largest whose final-position error against the
+    exact solution is no worse than the plain controller's, both at the given
+    quantile and at the maximum over the tracers. Returns (scale, table); the
+    scale is None if no candidate qualifies."""
+    ctx = ctx or _native.default_context()
+    rows = int(np.ceil(seconds / workload["params"]["gctimestep"])) + 4
+
+    def final(**over):
+        ens = Ensemble.from_workload(workload, "gc", max_rows=rows, ctx=ctx, **over)
+        st = ens.advance("gc", float(seconds))
+        h = ens.download()
+        if np.any(h["status"] != 0):
+            raise RuntimeError("calibration run stopped early: %s" % np.unique(h["status"]))
+        return h["s"][:3].T.copy(), st
+
+    exact, _ = final(rtol=1e-12, atol=1e-12, nsteps=1000000)
+    norm = np.linalg.norm(exact, axis=1)
+
+    def err_of(pos):
+        e = np.linalg.norm(pos - exact, axis=1) / norm
+        return {"median": float(np.median(e)), "q": float(np.quantile(e, quantile)), "max": float(e.max())}
+
+    pos, st = final(form=0)
+    plain = err_of(pos)
+    table = [{"scale": None, "form": 0, "rhs": int(st["rhs_evals"]), **plain}]
+    chosen = None
+    for sc in sorted(scales, reverse=True):
+        pos, st = final(form=form, learned_scale=float(sc), learned_every=int(every))
+        e = err_of(pos)
+        table.append({"scale": float(sc), "form": form, "rhs": int(st["rhs_evals"]), **e})
+        if e["q"] <= plain["q"] and e["max"] <= plain["max"]:
+            chosen = float(sc)
+            break
+    return chosen, table
 
 
 def calibrate(ctx, samples, margins=np.linspace(0.0, 1.0, 201)):

@@ -85,6 +85,30 @@ def test_collection_leaves_plain_results_unchanged(ctx):
     assert np.abs(np.median(s[:, 16])) < 0.5 and np.all(np.abs(s[:, 16]) < 30)
 
 
+def test_training_is_deterministic(ctx):
+    """Sample collection (appended in an order set by device atomics), the
+    canonical sort and device training repeated from scratch give the same
+    samples and bit-identical parameters; the gradient is reduced without
+    floating-point atomics."""
+    w = W.subsample(W.config2(), np.arange(0, 65536, 128))
+
+    def once():
+        ctx.mlp_samples_reserve(1 << 20, 1)
+        b = gpu_ensemble(w, "gc", max_rows=8, collect=1)
+        b.advance("gc", 3.0)
+        ctx.mlp_samples_sort()
+        s = ctx.mlp_samples_download()
+        p, losses = learned.train(ctx, steps=300, batch=2048, lr=2e-3, seed=4)
+        g, l = ctx.mlp_grad(s[:5000], switch_weight=1.0)
+        return s, p, losses, g, l
+
+    s1, p1, l1, g1, ll1 = once()
+    s2, p2, l2, g2, ll2 = once()
+    assert len(s1) > 10000 and np.array_equal(s1, s2)
+    assert np.array_equal(p1, p2) and l1 == l2
+    assert np.array_equal(g1, g2) and ll1 == ll2
+
+
 def _train_on_config2(ctx, seconds=10.0):
     """Plain then on-policy samples from the even-indexed tracers of a config-2
     subsample (2048 electrons, 10 s each round)."""
@@ -151,34 +175,69 @@ def test_learned_ab_against_plain(ctx, trained, oracle):
         assert r["glob_med"] < 3 * pl["glob_med"] and r["glob_max"] < 10 * pl["glob_max"], report
 
 
-def test_forms_error_at_bench_workload(ctx, trained, oracle):
-    """2,048 tracers of the 1M benchmark ensemble, one benchmark step (1 s):
-    relative final-position error of every form against the FP64 oracle."""
+BENCH_HORIZON = 25  # bench.py's advance(1.0) count in the standard run: 5 warm-up + 20 timed steps
+
+
+def test_forms_error_at_bench_workload(ctx, oracle):
+    """8,192 tracers of the 1M benchmark ensemble (evenly spaced), advanced by
+    the benchmark's whole run, 25 x advance(1.0), with the step model trained and
+    calibrated as bench.py does it: relative final-position error of every form
+    against the FP64 oracle and against the exact solution (a GPU run at rtol =
+    atol = 1e-12).
+
+    The plain form takes the oracle's step sequence; its difference is rounding,
+    amplified on a few sensitive orbits. The other forms take other step
+    sequences (the FP32 form occasionally, where rounding flips an accept/reject
+    decision; the learned forms always), and two valid rtol = 1e-8 solutions
+    differ by their integration errors: over 25 s the oracle's own global error
+    reaches ~4e-5 (max over the sample), so the learned forms' difference from
+    it cannot stay below 1e-6 there. What the learned forms keep is accuracy:
+    their global error against the exact solution is no worse than the plain
+    FP64 controller's (the scale is calibrated for that). After one benchmark
+    step (1 s) the learned + FP32 form is within 1e-6 of the oracle."""
+    import bench
     from tests._util import oracle_tracers
-    w0, p, info = trained
-    w = W.subsample(W.gc_bench(1 << 20), np.arange(0, 1 << 20, 512))
-    f, cfg, tr = oracle_tracers(oracle, w, "gc")
+    params, fit = bench.train_step_model(ctx)
+    ctx.mlp_set_params(params)
+    scale = fit["scale"]
+    w = W.gc_bench(1 << 20)
+    idx = bench.sample_indices(1 << 20, 8192)
+    ws = W.subsample(w, idx)
+    f, cfg, tr = oracle_tracers(oracle, ws, "gc")
     oracle.batch_advance(f, cfg, 1, tr, 1.0)
-    ctx.mlp_set_params(p)
-    errs = {}
+    orc1 = tr["s"][:, :3].copy()
+    oracle.batch_advance(f, cfg, 1, tr, float(BENCH_HORIZON - 1))
+    orc = tr["s"][:, :3]
+    exact, bad = bench.exact_positions(w, idx, BENCH_HORIZON, ctx)
+    assert bad == 0
+    res = {}
     for form in (PLAIN, FP32, LEARNED, LEARNED_FP32):
-        e = gpu_ensemble(w, "gc", max_rows=4, form=form, learned_scale=info["scale"])
+        e = gpu_ensemble(ws, "gc", max_rows=4, form=form, learned_scale=scale, learned_every=bench.LEARNED_EVERY)
         e.advance("gc", 1.0)
+        one = e.download()["s"][:3].T.copy()
+        for _ in range(BENCH_HORIZON - 1):
+            e.advance("gc", 1.0)
+            e.rows(reset=True)
         h = e.download()
         assert np.all(h["status"] == 0)
-        pos, _ = rel_state_error(h["s"], tr["s"], 4)
-        errs[form] = (float(np.median(pos)), float(np.percentile(pos, 99)), float(pos.max()))
-    print("bench-workload errors (median, p99, max)", errs)
-    # plain: rounding-level differences (a few orbits amplify them to ~1e-9)
-    assert errs[PLAIN][0] < 1e-12 and errs[PLAIN][2] < 1e-8
-    assert errs[FP32][0] < 1e-8 and errs[FP32][2] < 1e-6
-    # the learned forms take other (larger) steps: their difference is the
-    # integration error at rtol 1e-8. The target is 1e-6; the model is retrained
-    # per run from samples whose order (device atomics) varies, and the maximum
-    # over these 2,048 tracers has ranged 7.4e-7 .. 1.02e-6, so the bound is
-    # 1e-6 at the 99th percentile and 1.5e-6 at the maximum
+        pos = h["s"][:3].T
+        res[form] = {"oracle_1s": bench.pos_errors(one, orc1), "oracle": bench.pos_errors(pos, orc),
+                     "exact": bench.pos_errors(pos, exact)}
+    res["oracle_vs_exact"] = bench.pos_errors(orc, exact)
+    print("errors at the bench horizon", res, "scale", scale)
+    pl = res[PLAIN]
+    # plain: rounding-level differences from the oracle
+    assert pl["oracle"]["median"] < 1e-11 and pl["oracle"]["max"] < 1e-6, pl
+    assert pl["oracle_1s"]["max"] < 1e-8, pl
+    # FP32: the plain controller's steps except where rounding flips a decision
+    assert res[FP32]["oracle"]["median"] < 1e-6 and res[FP32]["oracle_1s"]["max"] < 1e-6, res[FP32]
+    # the learned forms: global error no worse than the plain form's (25 %
+    # allowance for the sample: the scale was calibrated on other tracers)
     for form in (LEARNED, LEARNED_FP32):
-        assert errs[form][1] < 1e-6 and errs[form][2] < 1.5e-6, (form, errs[form])
+        r = res[form]["exact"]
+        assert r["p99"] <= 1.25 * pl["exact"]["p99"] and r["max"] <= 1.25 * pl["exact"]["max"], (form, res)
+    # one benchmark step: the learned + FP32 form within 1e-6 of the oracle
+    assert res[LEARNED_FP32]["oracle_1s"]["max"] <= 1e-6, res[LEARNED_FP32]
 
 
 def test_switch_head_on_harris_adaptive(ctx):
