@@ -109,8 +109,8 @@ __global__ void __launch_bounds__(64) k_bc_interval(FieldP f, KParams P, int64_t
     double y1[3], k7[3], err;
     dopri5_attempt_rolled<3>(rhs, rt, y, k1, h, P.rtol, P.atol, y1, k7, err);
     nfcn += 6;
-    const double fac11 = pow(err, expo1);
-    double fac = fac11 / pow(facold, beta);
+    const double fac11 = pow_fp64(err, expo1);
+    double fac = fac11 / pow_fp64(facold, beta);
     fac = fmax(facc2, fmin(facc1, fac / safe));
     double hnew = h / fac;
     if (err <= 1.0) {

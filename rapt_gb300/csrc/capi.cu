@@ -12,6 +12,8 @@
 #include <string>
 #include <vector>
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include "launch.h"
 
 using namespace rapt;
@@ -42,6 +44,16 @@ struct Ctx {
   float *mlp_p = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_g = nullptr;
   double* mlp_loss = nullptr;
   uint32_t* mlp_w = nullptr;
+  // work-queue order (longest expected work first): sort keys and indices,
+  // the step totals at the start of the last call, CUB's sort storage
+  void* ord_block = nullptr;
+  uint32_t *ord_key_in = nullptr, *ord_key_out = nullptr;
+  int32_t *ord_idx_in = nullptr, *ord = nullptr;
+  int64_t* ord_steps = nullptr;
+  void* ord_tmp = nullptr;
+  size_t ord_tmp_bytes = 0;
+  float* mlp_partial = nullptr;  // [kMlpTrainMaxBlocks][kMlpGaccWords]
+  double* mlp_lpart = nullptr;   // [kMlpTrainMaxBlocks][2]
   bool mlp_ready = false;
   int64_t mlp_t = 0;  // Adam step count
   double* fl_scratch = nullptr;  // field-line traces of the bounce-period cadence
@@ -146,6 +158,9 @@ void finish_field(FieldP* f) {
     f->dh[i] = (float)k[i];
     f->dl[i] = (float)(k[i] - (double)f->dh[i]);
   }
+  f->gsh = (float)f->gradstep;
+  f->gsl = (float)(f->gradstep - (double)f->gsh);
+  f->inv2df = (float)f->inv2d;
 }
 
 // trace points per direction of the bounce-period field-line trace; a thread's
@@ -272,6 +287,7 @@ void rapt_ctx_destroy(void* ctx) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   cudaFree(c->block);
+  cudaFree(c->ord_block);
   cudaFree(c->scratch);
   cudaFree(c->tmp);
   cudaFree(c->mlp_block);
@@ -411,7 +427,32 @@ int rapt_ensemble_alloc(void* ctx, int64_t n, int32_t max_rows, int32_t max_swit
   CK(cudaStreamSynchronize(c->stream));
   cudaFree(c->block);
   c->block = nullptr;
+  cudaFree(c->ord_block);
+  c->ord_block = nullptr;
   c->n = 0;
+  if (n > 0x7fffffffLL) return fail(c, RAPT_ERR_INVALID, "at most 2^31 - 1 tracers per ensemble");
+  {
+    // queue-order buffers: keys and indices in and out, step totals, sort storage
+    const size_t N = (size_t)n;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    size_t cub_bytes = 0;
+    CK(cub::DeviceRadixSort::SortPairsDescending(nullptr, cub_bytes, (const uint32_t*)nullptr, (uint32_t*)nullptr,
+                                                 (const int32_t*)nullptr, (int32_t*)nullptr, (int)n));
+    const size_t ob = 4 * al(N * 4) + al(N * 8) + al(cub_bytes);
+    if (cudaMalloc(&c->ord_block, ob) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(c, RAPT_ERR_NOMEM, "cudaMalloc(%zu bytes) for the queue order failed", ob);
+    }
+    CK(cudaMemsetAsync(c->ord_block, 0, ob, c->stream));
+    char* q = static_cast<char*>(c->ord_block);
+    c->ord_key_in = carve<uint32_t>(q, N);
+    c->ord_key_out = carve<uint32_t>(q, N);
+    c->ord_idx_in = carve<int32_t>(q, N);
+    c->ord = carve<int32_t>(q, N);
+    c->ord_steps = carve<int64_t>(q, N);
+    c->ord_tmp = q;
+    c->ord_tmp_bytes = cub_bytes;
+  }
   const size_t bytes = ensemble_bytes(n, max_rows, max_switch);
   if (cudaMalloc(&c->block, bytes) != cudaSuccess) {
     cudaGetLastError();
@@ -451,6 +492,7 @@ int rapt_ensemble_alloc(void* ctx, int64_t n, int32_t max_rows, int32_t max_swit
   E.naccept = carve<int64_t>(p, N);
   E.nreject = carve<int64_t>(p, N);
   E.nfcn = carve<int64_t>(p, N);
+  E.order = nullptr;  // index order until the first advance sorts the queue
   c->n = n;
   c->max_rows = max_rows;
   c->max_sw = max_switch;
@@ -570,6 +612,7 @@ static DevEnsemble ensemble_view(const DevEnsemble& E, int64_t k, int max_rows, 
   V.nrows += k;
   V.sw_time += (size_t)k * max_sw;
   V.sw_mode += (size_t)k * max_sw;
+  V.order = nullptr;
   return V;
 }
 
@@ -583,6 +626,33 @@ int rapt_advance_resume(void* ctx, int kind, rapt_stats* stats) {
   Ctx* c = static_cast<Ctx*>(ctx);
   if (!c) return RAPT_ERR_INVALID;
   return advance_impl(c, kind, nullptr, 0.0, stats, true);
+}
+
+// Sort keys of the work queue: the RK attempts each tracer took in the previous
+// call (its step totals minus those at the start of that call), or, where none
+// are recorded (first call, state re-uploaded), an estimate from the state:
+// 1000 v / |x|, the transit rate that sets a guiding centre's steps.
+__global__ void k_order_keys(DevEnsemble E, int64_t* steps_prev, uint32_t* key, int32_t* idx) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= E.n) return;
+  const int64_t tot = E.naccept[k] + E.nreject[k];
+  const int64_t d = tot - steps_prev[k];
+  steps_prev[k] = tot;
+  uint32_t v;
+  if (d > 0) {
+    v = (uint32_t)min(d, (int64_t)0x7fffffff);
+  } else {
+    const double r = sqrt(E.s[0][k] * E.s[0][k] + E.s[1][k] * E.s[1][k] + E.s[2][k] * E.s[2][k]);
+    double speed = E.v[k];
+    if (E.mode[k] == RAPT_MODE_PARTICLE) {
+      const double p2 = E.s[3][k] * E.s[3][k] + E.s[4][k] * E.s[4][k] + E.s[5][k] * E.s[5][k];
+      speed = sqrt(p2) / sqrt(E.mass[k] * E.mass[k] + p2 / (kC * kC));
+    }
+    const double est = r > 0.0 ? 1000.0 * speed / r : 0.0;
+    v = (est >= 0.0 && est < 2.0e9) ? (uint32_t)est : 2000000000u;
+  }
+  key[k] = v;
+  idx[k] = (int32_t)k;
 }
 
 static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all, rapt_stats* stats, bool resume) {
@@ -651,6 +721,16 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
   if (resume) k_clear_rows_full<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(E);
   else k_prepare<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(E, d_delta, delta_all, kind);
   CK(cudaGetLastError());
+  if (!resume && !c->cfg.per_tracer_launches) {
+    // queue order for this call: longest expected work first (a resumed call
+    // keeps the order of the call it continues)
+    k_order_keys<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(E, c->ord_steps, c->ord_key_in, c->ord_idx_in);
+    CK(cudaGetLastError());
+    size_t tb = c->ord_tmp_bytes;
+    CK(cub::DeviceRadixSort::SortPairsDescending(c->ord_tmp, tb, c->ord_key_in, c->ord_key_out, c->ord_idx_in,
+                                                 c->ord, (int)c->n, 0, 32, s));
+    E.order = c->ord;
+  }
   CK(cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), s));
   int64_t launches = 0, kl = 1;
   const int max_rounds = 1000000;
@@ -820,7 +900,11 @@ int rapt_rhs_eval(void* ctx, int mode, int64_t n, const double* state, const dou
 static int mlp_ensure(Ctx* c) {
   if (c->mlp_block) return RAPT_OK;
   const size_t fl = (size_t)RAPT_MLP_NPARAMS * 4;
-  const size_t bytes = 4 * fl + 256 + (size_t)kMlpPackedWords * 4;
+  const size_t packed = ((size_t)kMlpPackedWords * 4 + 255) & ~size_t(255);
+  // parameters, Adam moments, gradient, loss words, packed weights, then the
+  // per-block gradient and loss partials of the deterministic reduction
+  const size_t bytes = 4 * fl + 256 + packed + (size_t)kMlpTrainMaxBlocks * kMlpGaccWords * 4 +
+                       (size_t)kMlpTrainMaxBlocks * 2 * 8;
   CK(cudaMalloc(&c->mlp_block, bytes));
   CK(cudaMemsetAsync(c->mlp_block, 0, bytes, c->stream));
   char* p = static_cast<char*>(c->mlp_block);
@@ -830,6 +914,8 @@ static int mlp_ensure(Ctx* c) {
   c->mlp_g = reinterpret_cast<float*>(p + 3 * fl);
   c->mlp_loss = reinterpret_cast<double*>(p + 4 * fl);
   c->mlp_w = reinterpret_cast<uint32_t*>(p + 4 * fl + 256);
+  c->mlp_partial = reinterpret_cast<float*>(p + 4 * fl + 256 + packed);
+  c->mlp_lpart = reinterpret_cast<double*>(p + 4 * fl + 256 + packed + (size_t)kMlpTrainMaxBlocks * kMlpGaccWords * 4);
   return RAPT_OK;
 }
 
@@ -895,7 +981,8 @@ int rapt_mlp_grad(void* ctx, const float* samples, int64_t n, float switch_weigh
   CK(cudaMemcpyAsync(d_s, samples, N * RAPT_MLP_SAMPLE * 4, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemsetAsync(c->mlp_g, 0, (size_t)RAPT_MLP_NTRAIN * 4, c->stream));
   CK(cudaMemsetAsync(c->mlp_loss, 0, 16, c->stream));
-  CK(mlp_grad(d_s, n, n, 0, 0, 0, switch_weight, c->mlp_w, c->mlp_p, c->mlp_g, c->mlp_loss, c->num_sms, c->stream));
+  CK(mlp_grad(d_s, n, n, 0, 0, 0, switch_weight, c->mlp_w, c->mlp_p, c->mlp_g, c->mlp_loss, c->mlp_partial,
+              c->mlp_lpart, c->stream));
   CK(cudaMemcpyAsync(grad, c->mlp_g, (size_t)RAPT_MLP_NTRAIN * 4, cudaMemcpyDeviceToHost, c->stream));
   double hl[2];
   CK(cudaMemcpyAsync(hl, c->mlp_loss, 16, cudaMemcpyDeviceToHost, c->stream));
@@ -975,6 +1062,32 @@ int rapt_mlp_samples_upload(void* ctx, const float* samples, int64_t n) {
   return RAPT_OK;
 }
 
+int rapt_mlp_samples_sort(void* ctx, int64_t first, int64_t n) {
+  Ctx* c = static_cast<Ctx*>(ctx);
+  if (!c || first < 0 || n < 0) return RAPT_ERR_INVALID;
+  if (!c->samp) return fail(c, RAPT_ERR_STATE, "no sample buffer");
+  CK(cudaSetDevice(c->device));
+  int64_t cnt = 0;
+  int rc = samples_count(c, &cnt);
+  if (rc) return rc;
+  if (first + n > cnt) return fail(c, RAPT_ERR_INVALID, "samples [%lld, %lld) beyond the %lld held", (long long)first,
+                                   (long long)(first + n), (long long)cnt);
+  if (n > 0x7fffffffLL) return fail(c, RAPT_ERR_INVALID, "at most 2^31 - 1 samples per sort");
+  if (n <= 1) return RAPT_OK;
+  const size_t bytes = mlp_sort_tmp_bytes(n);
+  void* tmp = nullptr;
+  if (cudaMalloc(&tmp, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, RAPT_ERR_NOMEM, "cudaMalloc(%zu bytes) for the sample sort failed", bytes);
+  }
+  const cudaError_t e = mlp_samples_sort(c->samp + (size_t)first * RAPT_MLP_SAMPLE, n, tmp, bytes, c->stream);
+  const cudaError_t e2 = cudaStreamSynchronize(c->stream);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return fail(c, RAPT_ERR_CUDA, "sample sort: %s", cudaGetErrorString(e));
+  if (e2 != cudaSuccess) return fail(c, RAPT_ERR_CUDA, "sample sort: %s", cudaGetErrorString(e2));
+  return RAPT_OK;
+}
+
 int rapt_mlp_train(void* ctx, int64_t steps, int32_t batch, float lr, float switch_weight, uint64_t seed,
                    double* loss) {
   Ctx* c = static_cast<Ctx*>(ctx);
@@ -991,7 +1104,7 @@ int rapt_mlp_train(void* ctx, int64_t steps, int32_t batch, float lr, float swit
     if (it == steps - tail) CK(cudaMemsetAsync(c->mlp_loss, 0, 16, c->stream));
     CK(cudaMemsetAsync(c->mlp_g, 0, (size_t)RAPT_MLP_NTRAIN * 4, c->stream));
     CK(mlp_grad(c->samp, cnt, batch, 1, seed, c->mlp_t, switch_weight, c->mlp_w, c->mlp_p, c->mlp_g,
-                it >= steps - tail ? c->mlp_loss : c->mlp_loss + 2, c->num_sms, c->stream));
+                it >= steps - tail ? c->mlp_loss : c->mlp_loss + 2, c->mlp_partial, c->mlp_lpart, c->stream));
     ++c->mlp_t;
     CK(mlp_adam(c->mlp_p, c->mlp_m, c->mlp_v, c->mlp_g, lr, c->mlp_t, c->stream));
     CK(mlp_pack(c->mlp_p, c->mlp_w, c->stream));

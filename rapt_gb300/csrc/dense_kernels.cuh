@@ -170,8 +170,8 @@ __global__ void __launch_bounds__(128) k_gc_dense(DevEnsemble E, KParams P, Scra
       dopri5_attempt_rolled<4, GcRHS<M>, true>(rhs, rt, y, k1, h, P.rtol, P.atol, y1, k7, err, dd);
       nfcn += 6;
       st.rhs += 6;
-      const double fac11 = pow(err, expo1);
-      double fac = fac11 / pow(facold, beta);
+      const double fac11 = pow_fp64(err, expo1);
+      double fac = fac11 / pow_fp64(facold, beta);
       fac = fmax(facc2, fmin(facc1, fac / safe));
       double hnew = h / fac;
       if (left_grid<M>(err)) {

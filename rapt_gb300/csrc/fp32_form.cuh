@@ -28,8 +28,6 @@ struct DFc {  // compile-time float-float constant
 __device__ __forceinline__ DF dfd(double v) { return df_from_double(v); }
 // model constant i of the FP32 form, precomputed on the host
 __device__ __forceinline__ DF fconst(const FieldP& f, int i) { return DF{f.dh[i], f.dl[i]}; }
-// small correction terms (finite-difference gradients): float precision suffices
-__device__ __forceinline__ DF dff(double v) { return DF{(float)v, 0.f}; }
 
 // ---------------------------------------------------------------- field models in float-float
 // Generic: FP64 model evaluated at the float-float point, rounded to float-float.
@@ -91,45 +89,53 @@ struct FieldDF<RAPT_DOUBLE_DIPOLE> {
 
 // grad|B| and curl b by the reference's central differences (fields.py:155-200,
 // the 6-point stencil of stencil_gradB_curlb): the six field samples, their
-// magnitudes and unit vectors in float-float (about 48 bits), the differences
-// of the samples in float-float (exact for these nearby values), and the
-// difference quotients in FP64. The samples' rounding adds about 1e-10
-// relative to the gradients, far below the stencil's own truncation error
-// ((gradstep / r)^2, about 4e-8 at 5 Re).
-// One stencil sample: |B| and B at x, float-float. Not inlined, so that the
-// kernel holds one copy of the field code for all six samples (the kernel runs
-// at high occupancy and its instruction cache is the limit).
+// magnitudes and unit vectors in float-float (about 48 bits) and the
+// differences of the samples in float-float (nearly exact for these nearby
+// values, so the cancellation that makes single-precision samples useless
+// loses nothing here); the difference quotients in FP32. Their consumer is the
+// FP32 drift term of the equations, and the stencil's own truncation error,
+// (gradstep / r)^2 = 4e-8 at 5 Re, is larger than FP32 rounding; an FP64
+// quotient would cost ~45 FP64 instructions per right-hand side on a pipe that
+// runs at 1/64 of the FP32 rate.
+// One stencil sample: |B| and the unit vector b at x, float-float. Not
+// inlined, so that the kernel holds one copy of the field code for all seven
+// samples of a right-hand side (the kernel runs at high occupancy and its
+// instruction cache is a limit); arguments and result pass by value, in
+// registers, not through local memory.
+struct DFSample {
+  DF mag, u0, u1, u2;
+};
 template <int M>
-__device__ __noinline__ void stencil_sample_df(const FieldP& f, double t, DF x0, DF x1, DF x2, DF* mag, DF* u) {
+__device__ __noinline__ DFSample stencil_sample_df(const FieldP& f, double t, DF x0, DF x1, DF x2) {
   const DF x[3] = {x0, x1, x2};
   DF b[3];
   FieldDF<M>::B(f, t, x, b);
   const DF s2 = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
   const DF ib = df_rsqrt(s2);
-  *mag = s2 * ib;
-  u[0] = b[0] * ib; u[1] = b[1] * ib; u[2] = b[2] * ib;
+  return DFSample{s2 * ib, b[0] * ib, b[1] * ib, b[2] * ib};
 }
 
 template <int M>
-__device__ __forceinline__ void stencil_gradB_curlb_df(const FieldP& f, double t, const DF* Y, double* gB,
-                                                       double* cb) {
-  const DF d = dfd(f.gradstep);
-  double c0 = 0.0, c1 = 0.0, c2 = 0.0;
+__device__ __forceinline__ void stencil_gradB_curlb_df(const FieldP& f, double t, const DF* Y, float* gB,
+                                                       float* cb) {
+  const DF d{f.gsh, f.gsl};
+  const float s = f.inv2df;
+  float c0 = 0.f, c1 = 0.f, c2 = 0.f;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     DF xp[3] = {Y[0], Y[1], Y[2]}, xm[3] = {Y[0], Y[1], Y[2]};
     xp[a] = Y[a] + d;
     xm[a] = Y[a] - d;
-    DF mp, mm, up[3], um[3];
-    stencil_sample_df<M>(f, t, xp[0], xp[1], xp[2], &mp, up);
-    stencil_sample_df<M>(f, t, xm[0], xm[1], xm[2], &mm, um);
-    gB[a] = df_to_double(mp - mm) * f.inv2d;
-    auto du = [&](int i) { return df_to_double(up[i] - um[i]); };
+    const DFSample sp = stencil_sample_df<M>(f, t, xp[0], xp[1], xp[2]);
+    const DFSample sm = stencil_sample_df<M>(f, t, xm[0], xm[1], xm[2]);
+    gB[a] = df_f(sp.mag - sm.mag) * s;
+    const DF up[3] = {sp.u0, sp.u1, sp.u2}, um[3] = {sm.u0, sm.u1, sm.u2};
+    auto du = [&](int i) { return df_f(up[i] - um[i]); };
     if (a == 0) { c1 -= du(2); c2 += du(1); }
     if (a == 1) { c0 += du(2); c2 -= du(0); }
     if (a == 2) { c0 -= du(1); c1 += du(0); }
   }
-  cb[0] = c0 * f.inv2d; cb[1] = c1 * f.inv2d; cb[2] = c2 * f.inv2d;
+  cb[0] = c0 * s; cb[1] = c1 * s; cb[2] = c2 * s;
 }
 
 // ---------------------------------------------------------------- right-hand sides
@@ -157,31 +163,56 @@ struct ParticleRHSdf {
 };
 
 // Guiding centre (Tao-Chan-Brizard, GuidingCenter.py:329-355), Y = (x, y, z [m],
-// u = ppar/(m c)). Centre field and the TCB algebra in float-float; grad|B|,
-// curl b and db/dt from the FP64 stencil of the plain form.
+// u = ppar/(m c)). Centre field and the TCB algebra in float-float; grad|B| and
+// curl b from the float-float stencil above (models with a float-float field),
+// or from the FP64 stencil and db/dt of the plain form (other models).
 template <int M>
 struct GcRHSdf {
-  FieldP f;
+  // the field parameters stay in the kernel's parameter space (the kernel takes
+  // them as __grid_constant__): the object handed to this non-inlined call holds
+  // a reference, not a ~260-byte copy written to local memory on every attempt
+  const FieldP& f;
   DF kmu, mcq, muq, qmc;  // 2 mu/(m c^2), m c/q, mu/q, q/(m c)
   bool eq;
-  // not inlined: one copy serves HINIT, the first slope and the rolled stages
-  __device__ __noinline__ void operator()(double t, const DF* Y, DF* o) const {
+  // The equations are one non-inlined function (one copy serves HINIT, the
+  // first slope and the rolled stages) taking and returning the state by value.
+  struct DF4 {
+    DF v0, v1, v2, v3;
+  };
+  __device__ __forceinline__ void operator()(double t, const DF* Y, DF* o) const {
+    const DF4 r = eval(t, DF4{Y[0], Y[1], Y[2], Y[3]});
+    o[0] = r.v0; o[1] = r.v1; o[2] = r.v2; o[3] = r.v3;
+  }
+  __device__ __noinline__ DF4 eval(double t, DF4 Yv) const {
+    const DF Y[4] = {Yv.v0, Yv.v1, Yv.v2, Yv.v3};
+    DF o[4];
     const DF u = Y[3];
-    DF B[3];
-    FieldDF<M>::B(f, t, Y, B);
-    const DF b2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
-    const DF ib = df_rsqrt(b2);
-    const DF Bmag = b2 * ib;
-    const DF ub[3] = {B[0] * ib, B[1] * ib, B[2] * ib};
-    double gBd[3], cbd[3], dbd[3];
+    DF B[3], Bmag, ub[3];
     if constexpr (FieldDF<M>::kDF) {
-      stencil_gradB_curlb_df<M>(f, t, Y, gBd, cbd);
-      dbd[0] = dbd[1] = dbd[2] = 0.0;
+      // the centre through the stencil's sample routine (one copy of the field
+      // code in the kernel), B = |B| b
+      const DFSample c = stencil_sample_df<M>(f, t, Y[0], Y[1], Y[2]);
+      Bmag = c.mag;
+      ub[0] = c.u0; ub[1] = c.u1; ub[2] = c.u2;
+      B[0] = ub[0] * Bmag; B[1] = ub[1] * Bmag; B[2] = ub[2] * Bmag;
+    } else {
+      FieldDF<M>::B(f, t, Y, B);
+      const DF b2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+      const DF ib = df_rsqrt(b2);
+      Bmag = b2 * ib;
+      ub[0] = B[0] * ib; ub[1] = B[1] * ib; ub[2] = B[2] * ib;
+    }
+    float gB[3], cb[3], db[3] = {0.f, 0.f, 0.f};
+    if constexpr (FieldDF<M>::kDF) {
       static_assert(!FieldDF<M>::kDF || Field<M>::kStatic, "float-float field models are static");
+      stencil_gradB_curlb_df<M>(f, t, Y, gB, cb);
     } else {
       const double Xd[3] = {df_to_double(Y[0]), df_to_double(Y[1]), df_to_double(Y[2])};
+      double gBd[3], cbd[3], dbd[3];
       stencil_gradB_curlb<M>(f, t, Xd, gBd, cbd);
       dbdt<M>(f, t, Xd, dbd);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) { gB[i] = (float)gBd[i]; cb[i] = (float)cbd[i]; db[i] = (float)dbd[i]; }
     }
     DF E[3];
     FieldDF<M>::E(f, t, Y, E);
@@ -191,8 +222,9 @@ struct GcRHSdf {
     const DF mg = muq * rg;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      Bs[i] = B[i] + pq * dff(cbd[i]);
-      Es[i] = E[i] - (pq * dff(dbd[i]) + mg * dff(gBd[i]));
+      Bs[i] = B[i] + pq * cb[i];
+      if constexpr (FieldDF<M>::kDF) Es[i] = E[i] - mg * gB[i];  // static: db/dt = 0
+      else Es[i] = E[i] - (pq * db[i] + mg * gB[i]);
     }
     const DF iBsp = df_rcp(Bs[0] * ub[0] + Bs[1] * ub[1] + Bs[2] * ub[2]);
     const DF Exb[3] = {Es[1] * ub[2] - Es[2] * ub[1], Es[2] * ub[0] - Es[0] * ub[2], Es[0] * ub[1] - Es[1] * ub[0]};
@@ -201,57 +233,18 @@ struct GcRHSdf {
     for (int i = 0; i < 3; ++i) o[i] = (a * Bs[i] + Exb[i]) * iBsp;
     o[3] = qmc * (Es[0] * Bs[0] + Es[1] * Bs[1] + Es[2] * Bs[2]) * iBsp;
     if (eq) { o[2] = DF{0.f, 0.f}; o[3] = DF{0.f, 0.f}; }
+    return DF4{o[0], o[1], o[2], o[3]};
   }
 };
 
 // ---------------------------------------------------------------- steps
-// Error term of one component: the plain form's norm on SI values.
-__device__ __forceinline__ double err_sk(DF y0, DF y1, double scale, double rtol, double atol) {
-  return atol + rtol * fmax(fabs(df_to_double(y0)), fabs(df_to_double(y1))) * scale;
-}
-
-// DOPRI5 attempt (same stages, error estimate and norm as dopri5_attempt).
-template <int NV, class F>
-__device__ __forceinline__ void dopri5_attempt_df(const F& f, double x, const DF* y, const DF* k1, double h,
-                                                  const double* scale, double rtol, double atol, DF* y1, DF* k7,
-                                                  double& err) {
-  using namespace dp5;
-  const DF hd = dfd(h);
-  DF k2[NV], k3[NV], k4[NV], k5[NV], k6[NV], yt[NV];
-#pragma unroll
-  for (int i = 0; i < NV; ++i) yt[i] = y[i] + hd * (k1[i] * DF(DFc(a21)));
-  f(x + c2 * h, yt, k2);
-#pragma unroll
-  for (int i = 0; i < NV; ++i) yt[i] = y[i] + hd * (k1[i] * DF(DFc(a31)) + k2[i] * DF(DFc(a32)));
-  f(x + c3 * h, yt, k3);
-#pragma unroll
-  for (int i = 0; i < NV; ++i)
-    yt[i] = y[i] + hd * (k1[i] * DF(DFc(a41)) + k2[i] * DF(DFc(a42)) + k3[i] * DF(DFc(a43)));
-  f(x + c4 * h, yt, k4);
-#pragma unroll
-  for (int i = 0; i < NV; ++i)
-    yt[i] = y[i] + hd * (k1[i] * DF(DFc(a51)) + k2[i] * DF(DFc(a52)) + k3[i] * DF(DFc(a53)) + k4[i] * DF(DFc(a54)));
-  f(x + c5 * h, yt, k5);
-#pragma unroll
-  for (int i = 0; i < NV; ++i)
-    yt[i] = y[i] + hd * (k1[i] * DF(DFc(a61)) + k2[i] * DF(DFc(a62)) + k3[i] * DF(DFc(a63)) +
-                         k4[i] * DF(DFc(a64)) + k5[i] * DF(DFc(a65)));
-  const double xph = x + h;
-  f(xph, yt, k6);
-#pragma unroll
-  for (int i = 0; i < NV; ++i)
-    y1[i] = y[i] + hd * (k1[i] * DF(DFc(a71)) + k3[i] * DF(DFc(a73)) + k4[i] * DF(DFc(a74)) +
-                         k5[i] * DF(DFc(a75)) + k6[i] * DF(DFc(a76)));
-  f(xph, y1, k7);
-  double e = 0.0;
-#pragma unroll
-  for (int i = 0; i < NV; ++i) {
-    const DF ei = k1[i] * DF(DFc(e1)) + k3[i] * DF(DFc(e3)) + k4[i] * DF(DFc(e4)) + k5[i] * DF(DFc(e5)) +
-                  k6[i] * DF(DFc(e6)) + k7[i] * DF(DFc(e7));
-    const double r = df_to_double(ei) * h * scale[i] / err_sk(y[i], y1[i], scale[i], rtol, atol);
-    e += r * r;
-  }
-  err = sqrt(e * (1.0 / NV));
+// Error ratio of one component, |e| / (atol + rtol max(|y0|, |y1|)), the plain
+// form's norm on SI values: e_si is the FP64 error estimate; the scale's |y| is
+// taken from the float parts (a tolerance scale needs a few digits) and the
+// quotient is a Newton-refined reciprocal (rcp_nr, ~1e-14).
+__device__ __forceinline__ double err_ratio(double e_si, DF y0, DF y1, double scale, double rtol, double atol) {
+  const float ym = fmaxf(fabsf(y0.hi), fabsf(y1.hi));
+  return e_si * rcp_nr(fma(rtol * scale, (double)ym, atol));
 }
 
 // The DOPRI5 tableau as float-float pairs in constant memory (rows as kDp5A).
@@ -272,7 +265,7 @@ static __constant__ DFpair kDp5Adf[7][6] = {
 // the right-hand side (float-float field, stencil and equations) is emitted
 // once instead of six times, which keeps the kernel inside the instruction
 // cache at the high occupancy this form runs at. The zero coefficients add
-// exact zeros, so the results equal dopri5_attempt_df's.
+// exact zeros.
 template <int NV, class F>
 __device__ __forceinline__ void dopri5_attempt_df_rolled(const F& f, double x, const DF* y, const DF* k1, double h,
                                                          const double* scale, double rtol, double atol, DF* y1,
@@ -306,10 +299,10 @@ __device__ __forceinline__ void dopri5_attempt_df_rolled(const F& f, double x, c
   for (int i = 0; i < NV; ++i) {
     const DF ei = k1[i] * DF(DFc(e1)) + k3[i] * DF(DFc(e3)) + k4[i] * DF(DFc(e4)) + k5[i] * DF(DFc(e5)) +
                   k6[i] * DF(DFc(e6)) + k7[i] * DF(DFc(e7));
-    const double r = df_to_double(ei) * h * scale[i] / err_sk(y[i], y1[i], scale[i], rtol, atol);
-    e += r * r;
+    const double r = err_ratio(df_to_double(ei) * (h * scale[i]), y[i], y1[i], scale[i], rtol, atol);
+    e = fma(r, r, e);
   }
-  err = sqrt(e * (1.0 / NV));
+  err = sqrt_nr(e * (1.0 / NV));
 }
 
 // DOP853 attempt.
@@ -376,7 +369,7 @@ __device__ __forceinline__ void dop853_attempt_df(const F& f, double x, const DF
     const DF bs = k1[i] * RAPT_C(b1) + k6[i] * RAPT_C(b6) + k7[i] * RAPT_C(b7) + k8[i] * RAPT_C(b8) +
                   k9[i] * RAPT_C(b9) + k10[i] * RAPT_C(b10) + k2[i] * RAPT_C(b11) + k3[i] * RAPT_C(b12);
     y1[i] = y[i] + hd * bs;
-    const double isk = scale[i] / err_sk(y[i], y1[i], scale[i], rtol, atol);
+    const double isk = err_ratio(scale[i], y[i], y1[i], scale[i], rtol, atol);
     const double r3 = df_to_double(bs - k1[i] * RAPT_C(bhh1) - k9[i] * RAPT_C(bhh2) - k3[i] * RAPT_C(bhh3)) * isk;
     const double r5 = df_to_double(k1[i] * RAPT_C(er1) + k6[i] * RAPT_C(er6) + k7[i] * RAPT_C(er7) +
                                    k8[i] * RAPT_C(er8) + k9[i] * RAPT_C(er9) + k10[i] * RAPT_C(er10) +
@@ -387,7 +380,7 @@ __device__ __forceinline__ void dop853_attempt_df(const F& f, double x, const DF
 #undef RAPT_C
   double deno = e5s + 0.01 * e3s;
   if (deno <= 0.0) deno = 1.0;
-  err = fabs(h) * e5s * sqrt(1.0 / (NV * deno));
+  err = fabs(h) * e5s * sqrt_nr(rcp_nr(NV * deno));
 }
 
 // HINIT with float-float right-hand sides; norms in FP64 on SI values.
@@ -419,15 +412,33 @@ __device__ __forceinline__ double hinit_df(const F& f, double x, const DF* y, co
   }
   der2 = sqrt(der2) / h;
   const double der12 = fmax(fabs(der2), sqrt(dnf));
-  const double h1 = (der12 <= 1e-15) ? fmax(1e-6, fabs(h) * 1e-3) : pow(0.01 / der12, iord_inv);
+  const double h1 = (der12 <= 1e-15) ? fmax(1e-6, fabs(h) * 1e-3) : pow_fp64(0.01 / der12, iord_inv);
   h = fmin(fmin(100.0 * fabs(h), h1), hmax);
   return copysign(h, posneg);
 }
 
-// err^p with FP32 exp2/log2 (relative error ~1e-7 of the factor).
-__device__ __forceinline__ double powf_fast(double err, float p) {
-  const float e = (float)fmax(err, 1e-30);
-  return (double)exp2f(p * __log2f(e));
-}
+// The step-size factors of the DOPRI5/DOP853 controller (Hairer's codes, as
+// SciPy's dopri5/dop853 run them) in FP32: fac11 = err^expo1, the Lund
+// stabilisation facold^-beta, the safety factor and the clamp; only the new
+// step h * factor is formed in FP64. A factor needs a few digits, and FP32
+// keeps its two logarithms, exponentials and quotients off the FP64 pipe.
+struct StepFactorF32 {
+  float inv_facold_beta;  // facold^-beta
+  float fac11;            // err^expo1 of the last attempt
+  __device__ __forceinline__ void reset(float beta) { inv_facold_beta = exp2f(-beta * __log2f(1e-4f)); }
+  // err of an attempt -> the factor h_new / h after acceptance
+  __device__ __forceinline__ float accept_factor(double err, float expo1, float safe, float facc1, float facc2) {
+    fac11 = exp2f(expo1 * __log2f((float)fmax(err, 1e-30)));
+    const float fac = fmaxf(facc2, fminf(facc1, fac11 * inv_facold_beta * __fdividef(1.f, safe)));
+    return __fdividef(1.f, fac);
+  }
+  // DOPRI5 rejection: h_new / h = 1 / min(facc1, fac11 / safe)
+  __device__ __forceinline__ float reject_factor(float safe, float facc1) const {
+    return __fdividef(1.f, fminf(facc1, fac11 * __fdividef(1.f, safe)));
+  }
+  __device__ __forceinline__ void accepted(double err, float beta) {
+    inv_facold_beta = exp2f(-beta * __log2f((float)fmax(err, 1e-4)));
+  }
+};
 
 }  // namespace rapt

@@ -25,12 +25,13 @@ __global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P,
   long long nacc = 0, nrej = 0, nfcn = 0;
   int status = 0, flags = 0, nrows = 0, nsw = 0, nseg = 0, nswitch = 0;
   bool k1_valid = false, seg_ok = true, in_interval = false;
-  double xend = 0, h = 0, facold_beta = 1, hmax = 0, posneg = 1;
+  double xend = 0, h = 0, hmax = 0, posneg = 1;
+  StepFactorF32 ctl{1.f, 1.f};
   bool reject = false, last = false;
   int nst = 0, nacc_int = 0;
 
-  constexpr double beta = 0.1, safe = 0.9;
-  constexpr double expo1 = 1.0 / 8.0 - beta * 0.2, facc1 = 1.0 / 0.3, facc2 = 1.0 / 6.0;
+  constexpr float beta = 0.1f, safe = 0.9f;
+  constexpr float expo1 = 1.0f / 8.0f - beta * 0.2f, facc1 = 1.0f / 0.3f, facc2 = 1.0f / 6.0f;
 
   auto state_si = [&](double* s) {
     for (int i = 0; i < 6; ++i) s[i] = df_to_double(y[i]) * scale[i];
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P,
     if (!in_interval) {
       if (!(seg_ok && rt < stop)) {
         bool more = false;
-        if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_OUT_OF_GRID &&
+        if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_OUT_OF_GRID && status != RAPT_ST_RKF_HMIN &&
             tcur < delta) {
           if (nseg + 1 >= P.max_segments) {
             status = RAPT_ST_ADAPTIVE_LIMIT;
@@ -126,7 +127,7 @@ __global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P,
       h = hinit_df<6>(rhs, rt, y, k1, scale, posneg, 1.0 / 8.0, hmax, P.rtol, P.atol);
       st.rhs++;
       nfcn += 2;
-      facold_beta = powf_fast(1e-4, (float)beta);
+      ctl.reset(beta);
       reject = false;
       last = false;
       in_interval = true;
@@ -145,15 +146,12 @@ __global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P,
       dop853_attempt_df<6>(rhs, rt, y, k1, h, scale, P.rtol, P.atol, y1, err);
       nfcn += 11;
       st.rhs += 11;
-      const double fac11 = powf_fast(err, (float)expo1);
-      double fac = fac11 / facold_beta;
-      fac = fmax(facc2, fmin(facc1, fac / safe));
-      double hnew = h / fac;
+      double hnew = h * (double)ctl.accept_factor(err, expo1, safe, facc1, facc2);
       if (left_grid<M>(err)) {
         ended = true;
         fail = RAPT_ST_OUT_OF_GRID;
       } else if (err <= 1.0) {
-        facold_beta = powf_fast(fmax(err, 1.0e-4), (float)beta);
+        ctl.accepted(err, beta);
         ++nacc; ++nacc_int; st.acc++;
         const double xph = rt + h;
         for (int i = 0; i < 6; ++i) y[i] = y1[i];
@@ -171,7 +169,7 @@ __global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P,
           h = hnew;
         }
       } else {
-        hnew = h / facc1;  // a rejected DOP853 step shrinks by dfactor, as SciPy's dop853 does
+        hnew = h * 0.3;  // a rejected DOP853 step shrinks by dfactor (h * 0.3), as SciPy's dop853 does
         reject = true;
         if (nacc_int >= 1) { ++nrej; st.rej++; }
         last = false;
@@ -185,8 +183,9 @@ __global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P,
       state_si(s);
       if (fail) { seg_ok = false; status = fail; }
       if (!all_finite<6>(s)) { seg_ok = false; status = RAPT_ST_NONFINITE; }
-      // a Grid step outside the grid: the reference raises inside the interval, adding no row
-      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID);
+      // a Grid step outside the grid (ValueError) or an RKF45 step below hmin
+      // (RuntimeError): the reference raises inside the interval, adding no row
+      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID) && status != RAPT_ST_RKF_HMIN;
       if (row) {
         t_row = rowt;
         tcur = rt + dt;
@@ -248,7 +247,8 @@ template <int M, int LRN = 0>
 // better than registers avoid the spills. Measured on the 1M guiding-centre
 // step: 1 block/SM 1.11e8 accepted steps/s, 8: 4.41e8, 12: 4.53e8, 16: 4.27e8
 // (the MLP variant: 12: 3.45e8, 16: 3.50e8).
-__global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E, KParams P, Scratch* S) {
+__global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E, const __grid_constant__ KParams P,
+                                                                     Scratch* S) {
   int64_t idx = -1;
   bool exhausted = false;
   long long budget = P.budget;
@@ -265,12 +265,13 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
   long long nacc = 0, nrej = 0, nfcn = 0;
   int status = 0, flags = 0, nrows = 0, nsw = 0, nseg = 0, nswitch = 0;
   bool k1_valid = false, seg_ok = true, in_interval = false;
-  double xend = 0, h = 0, facold_beta = 1, hmax = 0, posneg = 1;
+  double xend = 0, h = 0, hmax = 0, posneg = 1;
+  StepFactorF32 ctl{1.f, 1.f};
   bool reject = false, last = false;
   int nst = 0, nacc_int = 0;
 
-  constexpr double beta = 0.04, safe = 0.9;
-  constexpr double expo1 = 0.2 - beta * 0.75, facc1 = 1.0 / 0.2, facc2 = 1.0 / 10.0;
+  constexpr float beta = 0.04f, safe = 0.9f;
+  constexpr float expo1 = 0.2f - beta * 0.75f, facc1 = 1.0f / 0.2f, facc2 = 1.0f / 10.0f;
 
   auto state_si = [&](double* s) {
     for (int i = 0; i < 4; ++i) s[i] = df_to_double(y[i]) * scale[i];
@@ -343,7 +344,7 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
       if (!(seg_ok && rt < stop)) {
         bool more = false;
         if (P.kind == RAPT_KIND_ADAPTIVE && status != RAPT_ST_NONFINITE && status != RAPT_ST_BAD_INPUT &&
-            status != RAPT_ST_OUT_OF_GRID && tcur < delta) {
+            status != RAPT_ST_OUT_OF_GRID && status != RAPT_ST_RKF_HMIN && tcur < delta) {
           if (nseg + 1 >= P.max_segments) {
             status = RAPT_ST_ADAPTIVE_LIMIT;
           } else {
@@ -383,7 +384,7 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
         st.rhs++;
         nfcn += 2;
       }
-      facold_beta = powf_fast(1e-4, (float)beta);
+      ctl.reset(beta);
       errold = 1e-4;
       reject = false;
       last = false;
@@ -404,10 +405,7 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
       nfcn += 6;
       st.rhs += 6;
       lr.on_attempt(P, h, err, last);
-      const double fac11 = powf_fast(err, (float)expo1);
-      double fac = fac11 / facold_beta;
-      fac = fmax(facc2, fmin(facc1, fac / safe));
-      double hnew = h / fac;
+      double hnew = h * (double)ctl.accept_factor(err, expo1, safe, facc1, facc2);
       if (left_grid<M>(err)) {
         ended = true;
         fail = RAPT_ST_OUT_OF_GRID;
@@ -415,7 +413,7 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
         const double errprev = errold;
         const bool rej_before = reject;
         const double hstep = h;
-        facold_beta = powf_fast(fmax(err, 1.0e-4), (float)beta);
+        ctl.accepted(err, beta);
         errold = fmax(err, 1.0e-4);
         ++nacc; ++nacc_int; st.acc++;
         for (int i = 0; i < 4; ++i) { k1[i] = k7[i]; y[i] = y1[i]; }
@@ -435,7 +433,7 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
                      y[0].hi, y[1].hi, y[2].hi,
                      y[3].hi, vs, 1.0 - (xend - rt) / hmax);
       } else {
-        hnew = h / fmin(facc1, fac11 / safe);
+        hnew = h * (double)ctl.reject_factor(safe, facc1);
         reject = true;
         if (nacc_int >= 1) { ++nrej; st.rej++; }
         last = false;
@@ -449,8 +447,9 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
       state_si(s);
       if (fail) { seg_ok = false; status = fail; }
       if (!all_finite<4>(s)) { seg_ok = false; status = RAPT_ST_NONFINITE; }
-      // a Grid step outside the grid: the reference raises inside the interval, adding no row
-      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID);
+      // a Grid step outside the grid (ValueError) or an RKF45 step below hmin
+      // (RuntimeError): the reference raises inside the interval, adding no row
+      const bool row = !(M == RAPT_GRID && status == RAPT_ST_OUT_OF_GRID) && status != RAPT_ST_RKF_HMIN;
       if (row) {
         t_row = rt;
         tcur = rt;

@@ -100,7 +100,7 @@ __device__ __forceinline__ double hinit(const F& f, double x, const double* y, c
   }
   der2 = sqrt(der2) / h;
   const double der12 = fmax(fabs(der2), sqrt(dnf));
-  const double h1 = (der12 <= 1e-15) ? fmax(1e-6, fabs(h) * 1e-3) : pow(0.01 / der12, iord_inv);
+  const double h1 = (der12 <= 1e-15) ? fmax(1e-6, fabs(h) * 1e-3) : pow_fp64(0.01 / der12, iord_inv);
   h = fmin(fmin(100.0 * fabs(h), h1), hmax);
   return copysign(h, posneg);
 }

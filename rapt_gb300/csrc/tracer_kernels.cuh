@@ -223,7 +223,9 @@ struct LaneStats {
 
 // Warp-wide refill: every lane without a tracer takes the next queue index
 // until it holds a tracer of this kernel's mode or the queue is exhausted.
-// Must be called by all 32 lanes.
+// The queue runs over positions 0..n-1; E.order maps a position to a tracer
+// (longest expected work first, so that the lanes that finish last at the end
+// of a launch hold the shortest tracers). Must be called by all 32 lanes.
 template <class LoadFn>
 __device__ __forceinline__ void warp_refill(unsigned long long* queue, const DevEnsemble& E, int mode, int64_t& idx,
                                             bool& exhausted, LoadFn&& load) {
@@ -237,12 +239,15 @@ __device__ __forceinline__ void warp_refill(unsigned long long* queue, const Dev
     if (lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(m));
     base = __shfl_sync(kFull, base, leader);
     if (need) {
-      const unsigned long long k = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
-      if (k >= (unsigned long long)E.n) {
+      const unsigned long long q = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
+      if (q >= (unsigned long long)E.n) {
         exhausted = true;
-      } else if (E.mode[k] == mode && !(E.flags[k] & RAPT_FLAG_DONE) && E.status[k] != RAPT_ST_ROWS_FULL) {
-        idx = (int64_t)k;
-        load(idx);
+      } else {
+        const int64_t k = E.order ? (int64_t)E.order[q] : (int64_t)q;
+        if (E.mode[k] == mode && !(E.flags[k] & RAPT_FLAG_DONE) && E.status[k] != RAPT_ST_ROWS_FULL) {
+          idx = k;
+          load(idx);
+        }
       }
     }
   }
@@ -403,8 +408,8 @@ __global__ void __launch_bounds__(128) k_particle(DevEnsemble E, KParams P, Scra
         dop853_attempt<6>(rhs, rt, y, k1, h, P.rtol, P.atol, y1, err);
         nfcn += 11;
         st.rhs += 11;
-        const double fac11 = pow(err, expo1);
-        double fac = fac11 / pow(facold, beta);
+        const double fac11 = pow_fp64(err, expo1);
+        double fac = fac11 / pow_fp64(facold, beta);
         fac = fmax(facc2, fmin(facc1, fac / safe));
         double hnew = h / fac;
         if (left_grid<M>(err)) {
@@ -461,7 +466,7 @@ __global__ void __launch_bounds__(128) k_particle(DevEnsemble E, KParams P, Scra
           } else {
             ++nrej; st.rej++;
           }
-          h = h * fmin(fmax(0.84 * pow(P.rkf_tol / r, 0.25), 0.1), 4.0);
+          h = h * fmin(fmax(0.84 * pow_fp64(P.rkf_tol / r, 0.25), 0.1), 4.0);
           if (h > hmax) h = hmax;
           else if (h < P.rkf_hmin) { ended = true; fail = RAPT_ST_RKF_HMIN; }
           if (!ended && !(rt < xend)) ended = true;
@@ -694,8 +699,8 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
         nfcn += 6;
         st.rhs += 6;
         lr.on_attempt(P, h, err, last);
-        const double fac11 = pow(err, expo1);
-        double fac = fac11 / pow(facold, beta);
+        const double fac11 = pow_fp64(err, expo1);
+        double fac = fac11 / pow_fp64(facold, beta);
         fac = fmax(facc2, fmin(facc1, fac / safe));
         double hnew = h / fac;
         if (left_grid<M>(err)) {
@@ -755,7 +760,7 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
           } else {
             ++nrej; st.rej++;
           }
-          h = h * fmin(fmax(0.84 * pow(P.rkf_tol / r, 0.25), 0.1), 4.0);
+          h = h * fmin(fmax(0.84 * pow_fp64(P.rkf_tol / r, 0.25), 0.1), 4.0);
           if (h > hmax) h = hmax;
           else if (h < P.rkf_hmin) { ended = true; fail = RAPT_ST_RKF_HMIN; }
           if (!ended && !(rt < xend)) ended = true;
