@@ -9,12 +9,16 @@ equations, DOPRI5 at rtol = atol = 1e-8, GCtimestep 1 s. One step = one
 
 Four forms run on the same start state: plain FP64, FP32 stages, learned
 (FP64 with MLP step proposals) and learned+FP32. The step MLP is trained first
-(untimed) on guiding centres of an independent config-2 draw. ``value`` is the
-learned+FP32 form's whole-job accepted steps / device time with the state
-resident in HBM; ``forms`` holds every form's accepted steps/s, rejections,
-right-hand sides, simulated tracer-seconds/s and gyro-periods/s. ``e2e`` is
-the learned+FP32 metric through the public API with the state copied from
-pinned host memory and back inside the timed region. ``--impl reference``
+(untimed) on guiding centres of an independent config-2 draw, and its proposal
+scale is calibrated so that its global error matches the plain controller's.
+``value`` is the learned+FP32 form's whole-job accepted steps / device time
+with the state resident in HBM; ``forms`` holds every form's accepted steps/s,
+rejections, right-hand sides, simulated tracer-seconds/s and gyro-periods/s.
+``e2e`` is the learned+FP32 metric through the public API with the state copied
+from pinned host memory and back inside the timed region. ``accuracy``
+compares the final positions of an evenly spaced sample of the ensemble after
+the whole run (warm-up + timed steps) with the FP64 oracle (the CPU leg below)
+and with a tight-tolerance GPU run (the exact solution). ``--impl reference``
 times the CPU restatement of the reference algorithm (the oracle) on all host
 cores over a bounded sample of the same workload.
 """
@@ -40,11 +44,19 @@ UNIT = "accepted steps/s"
 # 446 flops (7-point stencil of 7 B evaluations) + 275 flops of stage
 # combination, error norm and control; rsqrt/sqrt/div/pow count as one flop each.
 FLOPS_PER_ACCEPTED_STEP = 6 * 446 + 275 + 6 * 23 + 4
-# DRAM traffic of one launch of the learned FP32 kernel per tracer and simulated
-# second (dram__bytes_read.sum + dram__bytes_write.sum of one ncu --set full
-# capture of the 262,144-tracer case: 198.8 + 221.5 GB), scaled by tracer count:
-# local-memory spill traffic of the 32-register, 16-blocks/SM configuration.
-TRAFFIC_PER_TRACER_SECOND = (198.8e9 + 221.5e9) / 262144
+# FP32-pipe thread instructions (FFMA + FADD + FMUL) per accepted step of the
+# FP32-form guiding-centre kernel k_gc32 in the double dipole: the float-float
+# stages, field samples and equations, from one ncu capture (sm__sass_thread_
+# inst_executed_op_{ffma,fadd,fmul}_pred_on.sum over the launch's accepted
+# steps; profiles/k_gc32_doubledipole_262k_full.md).
+FP32_OPS_PER_ACCEPTED_STEP = 24000
+# DRAM traffic of one k_gc32 launch per tracer and simulated second
+# (dram__bytes_read.sum + dram__bytes_write.sum of the same capture, local-memory
+# traffic; the algorithmic state traffic is ~464 B per tracer and launch).
+TRAFFIC_PER_TRACER_SECOND = 1.0e6
+# FP64 FMA issue rate of a GB300 SM (thread-instructions per clock; ncu's FP64
+# pipe peak, 304 per clock over the 152 SMs).
+FP64_FMA_PER_CLK_PER_SM = 2
 
 
 def parse():
@@ -65,13 +77,20 @@ def parse():
                          "earthdipole_particles (config 4) and compressed_adaptive (config 5): form comparisons "
                          "on --n tracers")
     ap.add_argument("--forms", default="plain,fp32,learned,learned_fp32",
-                    help="comma-separated forms to time (plain, fp32, learned, learned_fp32)")
+                    help="comma-separated forms to time (plain, fp32, learned, learned_fp32); the headline is "
+                         "learned_fp32 when listed")
+    ap.add_argument("--learned-every", type=int, default=LEARNED_EVERY,
+                    help="learned forms: network calls on every k-th accepted step (rapt_config.learned_every)")
+    ap.add_argument("--acc-sample", type=int, default=8192,
+                    help="tracers in the accuracy sample (evenly spaced; 0: no accuracy check)")
     return ap.parse_args()
 
 
 def dist_init(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    # the package's default context (field evaluations) on this rank's GPU
+    os.environ.setdefault("RAPT_DEVICE", os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch.distributed as dist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
@@ -150,32 +169,40 @@ class Clocks:
         return out
 
 
-def cpu_baseline(n_sample, threads):
-    """The oracle (CPU restatement of the reference algorithm) on host cores."""
+def sample_indices(n, n_sample):
+    return np.unique(np.linspace(0, n - 1, n_sample).astype(np.int64))
+
+
+def cpu_baseline(w, n_sample, horizon, threads):
+    """The oracle (CPU restatement of the reference algorithm) on host cores:
+    an evenly spaced sample of the guiding centres of workload `w` advanced
+    `horizon` seconds. Returns (accepted steps/s, accepted, seconds, final
+    states)."""
     from oracle import oracle as O
     from rapt_gb300 import workloads as W
-    w = W.gc_bench(1 << 20)
-    idx = np.linspace(0, len(w["mass"]) - 1, n_sample).astype(np.int64)
+    idx = sample_indices(len(w["mass"]), n_sample)
     w = W.subsample(w, idx)
     f = O.field("DoubleDipole")
     cfg = O.config(rtol=1e-8, atol=1e-8, gctimestep=1.0)
     tr = O.tracers_from_structs([O.gc_new_pa(f, w["pos"][i], w["v"][i], w["pa"][i], 0.0, w["mass"][i],
-                                             w["charge"][i]) for i in range(n_sample)])
+                                             w["charge"][i]) for i in range(len(idx))])
     t = time.perf_counter()
-    O.batch_advance(f, cfg, 1, tr, 1.0, nthreads=threads)
+    O.batch_advance(f, cfg, 1, tr, float(horizon), nthreads=threads)
     dt = time.perf_counter() - t
     acc = int(tr["naccept"].sum())
-    return acc / dt, acc, dt
+    return acc / dt, acc, dt, tr
 
 
 def run_reference(args, rank, ws, dist):
     if rank != 0:
         return
+    from rapt_gb300 import workloads as W
     threads = os.cpu_count() or 1
     n = args.cpu_sample or 16384
+    w = W.gc_bench(1 << 20)
     vals = []
     for i in range(args.warmup + args.steps):
-        v, acc, dt = cpu_baseline(n, threads)
+        v, acc, dt, _ = cpu_baseline(w, n, 1.0, threads)
         if i >= args.warmup:
             vals.append((acc, dt))
     acc = sum(a for a, _ in vals)
@@ -195,6 +222,7 @@ def run_reference(args, rank, ws, dist):
 
 FORMS = (("plain", 0), ("fp32", 1), ("learned", 2), ("learned_fp32", 3))
 HEADLINE = "learned_fp32"
+LEARNED_EVERY = 1  # the network runs on every k-th accepted step (rapt_config.learned_every)
 
 
 def gyro_frequency_sum(w, magB):
@@ -204,17 +232,43 @@ def gyro_frequency_sum(w, magB):
     return float(np.sum(np.abs(w["charge"]) * magB / (2 * np.pi * gamma * w["mass"])))
 
 
-def train_step_model(ctx, seconds=10.0):
+def train_step_model(ctx, every=None):
     """Trains the step MLP on guiding centres drawn from the config-2
     distributions (8,192 electrons, an independent draw from the benchmark's):
-    plain-controller samples then three on-policy rounds."""
+    plain-controller samples then three on-policy rounds, 10 s each; then the
+    proposal scale is calibrated on the global error of 1,024 other config-2
+    electrons over 10 s (learned.calibrate_global). Deterministic."""
     from rapt_gb300 import learned, workloads as W
     w = W.subsample(W.config2(), np.arange(0, 65536, 8))
     t = time.perf_counter()
-    p, info = learned.fit_gc(w, seconds, ctx=ctx, rounds=3, steps=3000, capacity=1 << 23, mask=7)
+    p, info = learned.fit_gc(w, 10.0, ctx=ctx, rounds=3, steps=3000, capacity=1 << 23, mask=7)
+    ctx.mlp_set_params(p)
+    wc = W.subsample(W.config2(), np.arange(4, 65536, 64))
+    scale, table = learned.calibrate_global(wc, 10.0, ctx=ctx, every=every or LEARNED_EVERY)
+    info["scale_samples"] = info["scale"]
+    info["calibration_global"] = table
+    info["scale"] = scale if scale is not None else min(r["scale"] for r in table if r["scale"] is not None)
     info["seconds"] = time.perf_counter() - t
     info["accepted_steps_generated"] = int(sum(c["accepted"] for c in info["collect"]))
     return p, info
+
+
+def pos_errors(pos, ref):
+    e = np.linalg.norm(pos - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    return {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)), "max": float(e.max())}
+
+
+def exact_positions(w, idx, horizon, ctx):
+    """Final positions of the sample tracers from a tight-tolerance run
+    (rtol = atol = 1e-12): the exact solution the forms' global errors are
+    measured against."""
+    from rapt_gb300 import Ensemble, workloads as W
+    ws = W.subsample(w, idx)
+    e = Ensemble.from_workload(ws, "gc", max_rows=int(horizon) + 4, ctx=ctx, rtol=1e-12, atol=1e-12,
+                               nsteps=1000000)
+    e.advance("gc", float(horizon))
+    h = e.download()
+    return h["s"][:3].T.copy(), int(np.count_nonzero(h["status"]))
 
 
 def run_ours(args, rank, ws, dist):
@@ -223,31 +277,52 @@ def run_ours(args, rank, ws, dist):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     ctx = N.Context(dev)
     fp64_peak, fp32_peak = ctx.measure_peaks()
-    params, fit = train_step_model(ctx)
-    ctx.mlp_set_params(params)
-    w = W.gc_bench(args.n, seed=rank)
+    forms = [(nm, f) for nm, f in FORMS if nm in args.forms.split(",")]
+    names = dict(forms)
+    if "plain" not in names:
+        raise SystemExit("--forms must include plain")
+    head = HEADLINE if HEADLINE in names else ("fp32" if "fp32" in names else "plain")
+    fit = None
+    every = args.learned_every
+    if "learned" in names or "learned_fp32" in names:
+        params, fit = train_step_model(ctx, every)
+        ctx.mlp_set_params(params)
+    if ws > 1:
+        # one ensemble of ws x n tracers, split into contiguous shards of equal
+        # estimated cost; rank r advances shard r
+        from rapt_gb300 import shard
+        w_all = W.gc_bench(args.n * ws)
+        field = F.DoubleDipole()
+        field.bind(ctx)
+        magB = field.magB(np.column_stack([np.zeros(len(w_all["mass"])), w_all["pos"]]))
+        costs = shard.cost_estimate(1, w_all["pos"], w_all["v"], w_all["mass"], w_all["charge"], magB, 1.0)
+        a, b = shard.shard(costs, rank, ws)
+        w = W.subsample(w_all, np.arange(a, b))
+        del w_all
+    else:
+        w = W.gc_bench(args.n)
     n = len(w["mass"])
     ens = Ensemble(F.DoubleDipole(), n, max_rows=4, ctx=ctx, pinned=not args.no_e2e)
     ens.configure(**w["params"])
     ens.set_guiding_centers(w["pos"], w["v"], pa=w["pa"], t0=0.0, mass=w["mass"], charge=w["charge"])
     init = {k: (v.copy()) for k, v in ens.h.items()}
     fgyro = gyro_frequency_sum(w, ens.field.magB(np.column_stack([np.zeros(n), w["pos"]])))
+    idx = sample_indices(n, args.acc_sample) if args.acc_sample > 0 else None
+    horizon = args.warmup + args.steps
+    scale = fit["scale"] if fit else 1.0
 
     def reset():
         for k, v in init.items():
             ens.h[k][...] = v
         ens.upload()
 
-    results = {}
-    forms = [(nm, f) for nm, f in FORMS if nm in args.forms.split(",")]
-    if "plain" not in dict(forms) or HEADLINE not in dict(forms):
-        raise SystemExit("--forms must include plain and %s" % HEADLINE)
+    results, finals = {}, {}
     barrier(dist)
     clk = Clocks(dev) if rank == 0 else None
     t_all = time.perf_counter()
     for name, form in forms:
         reset()
-        ens.configure(form=form, learned_scale=fit["scale"], collect=0)
+        ens.configure(form=form, learned_scale=scale, learned_every=every, collect=0)
         for _ in range(args.warmup):
             ens.advance("gc", 1.0)
             ens.rows(reset=True)
@@ -264,6 +339,9 @@ def run_ours(args, rank, ws, dist):
             launches += st["kernel_launches"]
             ens.ctx.check(ens.ctx.L.rapt_rows_download(ens.ctx.h, None, None, None, None, None, 1), "reset rows")
         barrier(dist)
+        if idx is not None:
+            h = ens.download()
+            finals[name] = (h["s"][:3, idx].T.copy(), int(np.count_nonzero(h["status"])))
         dev_s = allmax(dist, dev_ms * 1e-3)
         acc_all = allsum(dist, acc)
         sim = allsum(dist, float(n * args.steps))
@@ -275,7 +353,7 @@ def run_ours(args, rank, ws, dist):
                          "kernel_launches": int(launches), "device_ms": dev_ms}
     wall = time.perf_counter() - t_all
     clocks = clk.stop() if clk else None
-    head = results[HEADLINE]
+    headr = results[head]
     plain = results["plain"]
     for r in results.values():
         r["accepted_per_s_vs_plain"] = r["accepted_per_s"] / plain["accepted_per_s"]
@@ -284,7 +362,7 @@ def run_ours(args, rank, ws, dist):
     e2e = None
     if not args.no_e2e:
         reset()
-        ens.configure(form=dict(FORMS)[HEADLINE], learned_scale=fit["scale"])
+        ens.configure(form=names[head], learned_scale=scale, learned_every=every)
         h2d = sum(ens.h[k].nbytes for k in ens.h)
         d2h = h2d + n * ens.max_rows * 8 * 8  # state back + rows buffer
         barrier(dist)
@@ -298,44 +376,87 @@ def run_ours(args, rank, ws, dist):
             ens.rows(reset=True)
         e2e_s = allmax(dist, time.perf_counter() - t1)
         e2e = {"value": allsum(dist, acc_e) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "form": HEADLINE}
+               "d2h_bytes_per_step": int(d2h), "form": head}
+    gathered = None
+    if ws > 1:
+        # the host gather of every shard's final state (untimed)
+        from rapt_gb300 import shard
+        h = ens.download()
+        g = shard.gather(dist, {"s": h["s"][:4].T.copy(), "status": h["status"].copy(),
+                                "naccept": h["naccept"].copy()})
+        tot = shard.sum_counters(dist, {"tracers": n, "accepted": int(h["naccept"].sum())})
+        if rank == 0:
+            gathered = {"tracers": int(len(g["status"])), "failed": int(np.count_nonzero(g["status"])),
+                        "accepted_last_form": int(g["naccept"].sum()), "counters": tot,
+                        "shards": "contiguous, balanced by estimated cost (rapt_gb300.shard)"}
     if rank != 0:
         return
-    achieved = FLOPS_PER_ACCEPTED_STEP * head["accepted"] / (head["device_ms"] * 1e-3) / 1e12
-    achieved_plain = FLOPS_PER_ACCEPTED_STEP * plain["accepted"] / (plain["device_ms"] * 1e-3) / 1e12
-    line = {"metric": METRIC, "value": head["accepted_per_s"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 stages (float-float) + f64 control/stencil",
+    # ---- roofline: each kernel against the pipe it runs on
+    import torch
+    num_sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    fp64_spec = num_sms * FP64_FMA_PER_CLK_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    plain_tf = FLOPS_PER_ACCEPTED_STEP * plain["accepted"] / (plain["device_ms"] * 1e-3) / 1e12
+    roof_plain = {"kernel": "k_gc<DoubleDipole> (plain FP64)", "bound": "fp64", "unit": "TFLOP/s",
+                  "achieved": plain_tf, "peak": fp64_spec, "frac": plain_tf / fp64_spec,
+                  "peak_note": "%d SMs x %d FP64 FMA/clk x 2 flops x %.0f MHz (sampled SM clock)" % (
+                      num_sms, FP64_FMA_PER_CLK_PER_SM, sm_mhz),
+                  "peak_microbench": fp64_peak, "frac_microbench": plain_tf / fp64_peak,
+                  "flops_per_accepted_step": FLOPS_PER_ACCEPTED_STEP,
+                  "flops_note": "algorithmic FP64 flops of one DOPRI5 step (FMA = 2, rsqrt/div/pow = 1)"}
+    line = {"metric": METRIC, "value": headr["accepted_per_s"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": headr["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 stages (float-float) + f64 control" if head != "plain" else "f64",
             "data": "synthetic (seeded, config-2 distributions at 2^20 tracers per GPU)",
-            "config": {"workload": "gc_doubledipole_1M", "tracers_per_gpu": n, "form": HEADLINE,
+            "config": {"workload": "gc_doubledipole_1M", "tracers_per_gpu": n, "form": head,
                        "eom": "TaoChanBrizard", "method": "DOPRI5", "rtol": 1e-8, "atol": 1e-8,
                        "step": "GuidingCenter.advance(1.0) of every tracer",
                        "l2": "state 1M x 232 B > L2 (compute bound; no flush)",
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
-            "forms": results,
-            "step_model": {"scale": fit["scale"], "train_seconds": fit["seconds"],
-                           "accepted_steps_generated": fit["accepted_steps_generated"],
-                           "samples": int(sum(c["samples"] for c in fit["collect"])),
-                           "calibration": fit["calibration"][-1], "losses": fit["losses"][-1]},
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": achieved / fp64_peak, "traffic": TRAFFIC_PER_TRACER_SECOND * n,
-                         "traffic_note": "bytes per launch, scaled from a 262,144-tracer ncu capture; "
-                                         "spill traffic (algorithmic state traffic ~464 B per tracer)",
-                         "kernel": "k_gc32 (learned)",
-                         "peak_source": "measured in-run: FP64 FMA chains (rapt_measure_peaks)",
-                         "flops_per_accepted_step": FLOPS_PER_ACCEPTED_STEP,
-                         "flops_note": "algorithmic FP64-equivalent flops of one DOPRI5 step",
-                         "plain_kernel": {"kernel": "k_gc", "achieved": achieved_plain,
-                                          "frac": achieved_plain / fp64_peak},
-                         "fp32_peak_tflops": fp32_peak},
-            "gpu_launches": int(head["kernel_launches"]), "clocks": clocks, "wall_s": wall}
+                       "parallelism": "%d cost-balanced shards of one ensemble" % ws if ws > 1 else "single GPU"},
+            "forms": results, "gpu_launches": int(headr["kernel_launches"]), "clocks": clocks, "wall_s": wall}
+    if head in ("fp32", "learned_fp32"):
+        ops = FP32_OPS_PER_ACCEPTED_STEP * headr["accepted"] / (headr["device_ms"] * 1e-3) / 1e12
+        fp32_ops_peak = fp32_peak / 2  # the microbenchmark counts an FMA as 2 flops
+        traffic = TRAFFIC_PER_TRACER_SECOND * n
+        line["roofline"] = {"kernel": "k_gc32<DoubleDipole> (%s)" % head, "bound": "fp32", "unit": "Tops/s",
+                            "achieved": ops, "peak": fp32_ops_peak, "frac": ops / fp32_ops_peak,
+                            "ops_per_accepted_step": FP32_OPS_PER_ACCEPTED_STEP,
+                            "ops_note": "FP32-pipe thread instructions (FFMA/FADD/FMUL) per accepted step, from ncu",
+                            "peak_source": "measured in-run: FP32 FMA chains (rapt_measure_peaks)",
+                            "traffic": traffic, "traffic_note": "DRAM bytes per launch (local memory), "
+                            "scaled from a 262,144-tracer ncu capture",
+                            "traffic_frac_hbm": traffic / (headr["ms_per_step"] * 1e-3) / 6788.3e9,
+                            "plain_kernel": roof_plain}
+    else:
+        line["roofline"] = dict(roof_plain)
+    if fit:
+        line["step_model"] = {"scale": fit["scale"], "scale_from_samples": fit["scale_samples"],
+                              "learned_every": every, "train_seconds": fit["seconds"],
+                              "accepted_steps_generated": fit["accepted_steps_generated"],
+                              "samples": int(sum(c["samples"] for c in fit["collect"])),
+                              "calibration": fit["calibration"][-1], "calibration_global": fit["calibration_global"],
+                              "losses": fit["losses"][-1]}
     if e2e:
         line["e2e"] = e2e
+    if gathered:
+        line["gather"] = gathered
     if not args.no_cpu_baseline:
-        n_s = args.cpu_sample or 65536
-        v, a, dt = cpu_baseline(n_s, os.cpu_count() or 1)
+        v, a, dt, tr = cpu_baseline(w, len(idx) if idx is not None else 4096, horizon, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                "sample": "%d of the 1,048,576 tracers, 1 s each (%.1f s)" % (n_s, dt)}
+                                "sample": "%d of the %d tracers (evenly spaced), %d s each (%.1f s)" % (
+                                    len(tr), n, horizon, dt)}
+        if idx is not None:
+            exact, bad = exact_positions(w, idx, horizon, ctx)
+            orc = tr["s"][:, :3]
+            line["accuracy"] = {
+                "sample_tracers": int(len(idx)), "horizon_s": horizon,
+                "measure": "relative final-position error |dx| / |x| after warm-up + timed steps",
+                "vs_oracle": {k: pos_errors(v[0], orc) for k, v in finals.items()},
+                "vs_exact": {k: pos_errors(v[0], exact) for k, v in finals.items()},
+                "oracle_vs_exact": pos_errors(orc, exact),
+                "exact": "GPU plain FP64 at rtol = atol = 1e-12", "failed": {k: v[1] for k, v in finals.items()},
+                "exact_failed": bad}
     print(json.dumps(line), flush=True)
 
 

@@ -81,3 +81,14 @@ def test_noalloc_refuses_before_touching_the_device():
     assert call(gctimestep=-1.0) == N.RAPT_ERR_INVALID
     st.n = N.NOALLOC_MAX_TRACERS + 1
     assert call() == N.RAPT_ERR_INVALID
+
+
+def test_object_api_raises_like_the_reference_on_stepper_failures():
+    """A tracer that stopped because the RKF45 step fell below hmin raises
+    RuntimeError (rkf.py:136-139); one that left a Grid raises ValueError."""
+    from rapt_gb300 import tracers as T
+    with pytest.raises(RuntimeError):
+        T._raise_if_left_grid({"status": [N.ST["RKF_HMIN"]]})
+    with pytest.raises(ValueError):
+        T._raise_if_left_grid({"status": [N.ST["OUT_OF_GRID"]]})
+    T._raise_if_left_grid({"status": [0]})
