@@ -80,7 +80,8 @@ def parse():
                     help="comma-separated forms to time (plain, fp32, learned, learned_fp32); the headline is "
                          "learned_fp32 when listed")
     ap.add_argument("--learned-every", type=int, default=LEARNED_EVERY,
-                    help="learned forms: network calls on every k-th accepted step (rapt_config.learned_every)")
+                    help="learned forms: the network runs on every k-th step-loop iteration of a warp "
+                         "(rapt_config.learned_every)")
     ap.add_argument("--acc-sample", type=int, default=8192,
                     help="tracers in the accuracy sample (evenly spaced; 0: no accuracy check)")
     return ap.parse_args()
@@ -222,7 +223,7 @@ def run_reference(args, rank, ws, dist):
 
 FORMS = (("plain", 0), ("fp32", 1), ("learned", 2), ("learned_fp32", 3))
 HEADLINE = "learned_fp32"
-LEARNED_EVERY = 1  # the network runs on every k-th accepted step (rapt_config.learned_every)
+LEARNED_EVERY = 1  # the network runs on every k-th step-loop iteration of a warp (rapt_config.learned_every)
 
 
 def gyro_frequency_sum(w, magB):
@@ -553,24 +554,36 @@ def run_forms_workload(args, rank, ws, dist):
     else:
         w = W.subsample(W.config5(seed=rank), np.arange(0, 1 << 20, max(1, (1 << 20) // n))[:n])
         kind, delta, rows = "adaptive", 200.0, 1024
-        forms = list(FORMS)
-        params, fit = train_step_model(ctx)
-        ctx.mlp_set_params(params)
-        scale = fit["scale"]
+        forms = [(nm, f) for nm, f in FORMS if nm in args.forms.split(",")]
+        if any(f >= 2 for _, f in forms):
+            params, fit = train_step_model(ctx, args.learned_every)
+            ctx.mlp_set_params(params)
+            scale = fit["scale"]
+        else:
+            scale = 1.0
     ens = Ensemble.from_workload(w, kind, max_rows=rows, max_switch=64, ctx=ctx)
     init = {k: v.copy() for k, v in ens.h.items()}
     sim = float(np.sum(np.broadcast_to(delta, (len(w["mass"]),))))
-    res = {}
+    res, finals = {}, {}
+    if kind == "particle":
+        p0 = np.linalg.norm(init["s"][3:6].T, axis=1)
     for name, form in forms:
         for k, v in init.items():
             ens.h[k][...] = v
         ens.upload()
         if kind == "adaptive":
             ens.adaptive_init()
-        ens.configure(form=form, learned_scale=scale)
+        ens.configure(form=form, learned_scale=scale, learned_every=args.learned_every)
         barrier(dist)
         st = advance_all(ens, kind, delta)
         h = ens.download()
+        finals[name] = (h["s"][:3].T.copy(), h["status"].copy(), h["mode"].copy())
+        if kind == "particle":
+            # kinetic-energy drift: |p| is conserved in the static dipole
+            p1 = np.linalg.norm(h["s"][3:6].T, axis=1)
+            drift = np.abs(p1 / p0 - 1.0)[h["status"] == 0]
+            energy_drift = {"median": float(np.median(drift)), "p99": float(np.percentile(drift, 99)),
+                            "max": float(drift.max())}
         dev_s = allmax(dist, st["kernel_ms"] * 1e-3)
         res[name] = {"device_s": dev_s, "accepted": int(st["accepted"]), "rejected": int(st["rejected"]),
                      "reject_rate": st["rejected"] / max(st["accepted"], 1),
@@ -581,11 +594,24 @@ def run_forms_workload(args, rank, ws, dist):
                      "naccept_per_tracer": {"median": float(np.median(h["naccept"])),
                                             "p99": float(np.percentile(h["naccept"], 99)),
                                             "max": int(h["naccept"].max())}}
+        if kind == "particle":
+            res[name]["energy_drift"] = energy_drift
     if rank != 0:
         return
     plain = res["plain"]
     for r in res.values():
         r["tracer_seconds_per_s_vs_plain"] = r["tracer_seconds_per_s"] / plain["tracer_seconds_per_s"]
+    # error against the plain FP64 form on the same ensemble (tracers that both
+    # finished without a failure status)
+    p_pos, p_st, p_mode = finals["plain"]
+    for name, (pos, st_, mode) in finals.items():
+        if name == "plain":
+            continue
+        ok = (st_ == 0) & (p_st == 0)
+        e = np.linalg.norm(pos[ok] - p_pos[ok], axis=1) / np.linalg.norm(p_pos[ok], axis=1)
+        res[name]["error_vs_plain"] = {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)),
+                                       "max": float(e.max()), "compared": int(ok.sum()),
+                                       "same_final_mode": int(np.sum(ok & (mode == p_mode)))}
     print(json.dumps({"workload": args.workload, "tracers_per_gpu": len(w["mass"]), "n_gpus": ws,
                       "kind": kind, "sim_tracer_seconds": sim, "results": res}), flush=True)
 

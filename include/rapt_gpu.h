@@ -104,8 +104,10 @@ typedef struct {
                                     graph and replay it until no tracer is pending */
   int32_t collect;               /* 1: record step-size training samples (GC, DOPRI5; any form) */
   double learned_scale;          /* learned forms: multiplier on each MLP step proposal (0: 1) */
-  int32_t learned_every;         /* learned forms: run the MLP on every k-th accepted step and reuse its
-                                    correction in between (0 or 1: every step) */
+  int32_t learned_every;         /* learned forms: a warp runs the MLP on every k-th iteration of its step
+                                    loop, for the lanes that accepted a step since its last call; each lane
+                                    scales the controller's steps by its latest correction (0 or 1: every
+                                    iteration) */
   int32_t per_tracer_launches;   /* 1: one launch sequence per tracer (the unbatched pattern, for
                                     comparison); 0: one persistent grid for the whole ensemble */
   double bounceresolution;       /* params["bounceresolution"]: with gctimestep == 0 the GC cadence is

@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
   for (;;) {
     warp_refill(&S->queue[1], E, RAPT_MODE_GC, idx, exhausted, load);
     if (__all_sync(kFull, idx < 0)) break;
-    lr.infer(P, h, in_interval);
+    lr.infer(P);
     if (idx < 0) continue;
 
     const GcRHSdf<M> rhs{P.f, kmu, mcq, muq, qmc, P.enforce_eq != 0};

@@ -263,9 +263,8 @@ struct StepLearner {
     return LRN == 0 ? 0 : kRawOff + ((LRN == 1 || collect) ? 32 * 16 : 0);
   }
   float c_mass, c_energy, c_sign, c_pitch;  // per-tracer feature constants
-  float rcap;                               // cap on the learned correction
-  float rlast;                              // last correction of the network (reused between calls)
-  int since;                                // accepted steps since the last network call
+  float rlast;                              // this lane's latest correction from the network (1: none yet)
+  unsigned wit;                             // loop iterations of the warp (warp-uniform)
   double hbase;                             // collect: the controller's step after the sampled step
   double hcont;                             // learned: the step wanted before the interval-end clip
   bool want, pend, pend_sw, have_prop;
@@ -274,14 +273,13 @@ struct StepLearner {
   __device__ __forceinline__ void init(const KParams& P) {
     want = pend = pend_sw = have_prop = false;
     rlast = 1.f;
-    since = 0;
+    wit = 0;
     sm = LRN ? rapt_dyn_smem + (threadIdx.x >> 5) * warp_words(P.collect != 0) : nullptr;
   }
   // Per-tracer constants; vs is the speed, pitch scale converts ppar to cos(pitch).
   __device__ __forceinline__ void load(double mass, double charge, double vs, double ppar_unit) {
     want = pend = pend_sw = have_prop = false;
     rlast = 1.f;
-    since = 0;
     if constexpr (LRN != 0) {
       const double gam = 1.0 / sqrt(1.0 - (vs / kC) * (vs / kC));
       c_mass = log10f((float)(mass / kMe));
@@ -298,6 +296,9 @@ struct StepLearner {
   // step hnew) ending at position pos with parallel momentum ppar. A step that
   // ended an output interval gives no sample; the learned form continues the
   // next interval with the step wanted before the clip (in place of HINIT).
+  // The learned form scales hnew by the lane's latest correction from the
+  // network (capped at hmax and, after a rejection, at the last accepted step)
+  // and stages this step's features for the warp's next network call (infer).
   // `allow` switches the proposals off (the plain controller takes over) for
   // the rest of an output interval that has seen many rejections. A step that
   // ends an interval whose row gets an adiabaticity check (`row_check`) stages
@@ -319,14 +320,12 @@ struct StepLearner {
       coll = (LRN == 1 || P.collect) &&
              (mix64((uint64_t)idx * 0x100000001b3ull + (uint64_t)nacc) & P.samp_mask) == 0;
     }
-    bool inf = LRN == 2 && allow && !last;
+    const bool inf = LRN == 2 && allow && !last;
     if constexpr (LRN == 2) {
-      if (inf && P.learn_every > 1 && ++since < P.learn_every) {
-        // between network calls: the last correction on the controller's step
+      if (inf) {
         float cap = (float)(hmax / fabs(hnew));
         if (rej_before) cap = fminf(cap, (float)(fabs(h) / fabs(hnew)));
         hnew *= (double)fminf(rlast, cap);
-        inf = false;
       }
     }
     if (!coll && !coll_sw && !inf) return;
@@ -361,9 +360,6 @@ struct StepLearner {
       if (inf) {
         stage_features(P.mlp_p, f, sm, lane);
         want = true;
-        float cap = (float)(hmax / fabs(hnew));
-        if (rej_before) cap = fminf(cap, (float)(fabs(h) / fabs(hnew)));
-        rcap = cap;
       }
     }
   }
@@ -403,21 +399,21 @@ struct StepLearner {
       }
     }
   }
-  // Learned: warp-collective inference for the lanes that staged features;
-  // scales their next step h. Called by all 32 lanes at the top of the loop.
-  __device__ __forceinline__ void infer(const KParams& P, double& h, bool in_interval) {
+  // Learned: warp-collective inference, on every learn_every-th iteration of
+  // the warp's loop, for the lanes that staged features since the last call;
+  // refreshes their correction (used from their next accepted step on). One
+  // call serves every lane that accepted a step in between, so its cost is
+  // spread over learn_every iterations. Called by all 32 lanes at the top of
+  // the loop.
+  __device__ __forceinline__ void infer(const KParams& P) {
     if constexpr (LRN == 2) {
-      if (__any_sync(kFull, want)) {
+      ++wit;
+      if (wit % (unsigned)P.learn_every == 0u && __any_sync(kFull, want)) {
         float o[2];
         mlp_forward_staged(P.mlp_w, P.mlp_p, sm, o);
-        if (want) {
-          const float rn = __expf(fminf(fmaxf(o[0], -3.f), 3.f)) * P.learn_scale;
-          rlast = rn;
-          since = 0;
-          h *= (double)fminf(rn, rcap);
-        }
+        if (want) rlast = __expf(fminf(fmaxf(o[0], -3.f), 3.f)) * P.learn_scale;
+        want = false;
       }
-      want = false;
     }
   }
 };

@@ -35,7 +35,8 @@ def _config(eom=0, tableau=0):
     return dict(rtol=rtol, atol=atol, cyclotronresolution=p["cyclotronresolution"], gctimestep=p["GCtimestep"],
                 epss=p["epss"], epst=p["epst"], enforce_equatorial=int(bool(p["enforce equatorial"])),
                 gc_eom=eom, tableau=tableau, bounceresolution=p["bounceresolution"],
-                fieldlineresolution=p["fieldlineresolution"], dense_output=int(bool(p.get("dense output", False))))
+                fieldlineresolution=p["fieldlineresolution"], dense_output=int(bool(p.get("dense output", False))),
+                rkf_tol=float(p.get("rkf tolerance", 1e-3)), rkf_hmin=float(p.get("rkf minimum step", 1e-12)))
 
 
 class _Pickle:

@@ -1,7 +1,8 @@
 """Sharding one ensemble over ranks (rapt_gb300.shard) on the host, no GPU:
 the cost-balanced contiguous partition, and with two gloo ranks the gather of
-per-shard final states to rank 0 and the sum of counters -- the same calls
-bench.py's own arm makes under torchrun. The advance of each shard is replaced
+per-shard final states to rank 0, the sum of counters and bench.py's timing
+reductions (max over ranks, sums) -- the calls bench.py's own arm makes under
+torchrun. The advance of each shard is replaced
 by a deterministic host function of the state, which is all the sharding logic
 can see of it."""
 import os
@@ -66,6 +67,7 @@ def _fake_advance(st):
 
 def _worker(rank, world, port, q):
     import torch.distributed as dist
+    import bench
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
@@ -76,12 +78,15 @@ def _worker(rank, world, port, q):
         out = _fake_advance(mine)
         tot = shard.sum_counters(dist, {"accepted": int(out["naccept"].sum()), "tracers": b - a})
         g = shard.gather(dist, out)
+        # bench.py's timing reductions: the slowest rank's time, the summed work
+        red = (bench.allmax(dist, 1.0 + rank), bench.allsum(dist, float(b - a)))
+        bench.barrier(dist)
         if rank == 0:
-            q.put(("ok", g, tot))
+            q.put(("ok", g, tot, red))
         else:
-            q.put(("rank", g is None, tot))
+            q.put(("rank", g is None, tot, red))
     except Exception as e:  # report instead of hanging the parent
-        q.put(("err", repr(e), None))
+        q.put(("err", repr(e), None, None))
     finally:
         dist.destroy_process_group()
 
@@ -106,3 +111,4 @@ def test_gather_and_counters_two_gloo_ranks():
     g = ok[1]
     assert np.array_equal(g["x"], ref["x"]) and np.array_equal(g["naccept"], ref["naccept"])
     assert ok[2] == other[2] == {"accepted": int(ref["naccept"].sum()), "tracers": 1000}
+    assert ok[3] == other[3] == (2.0, 1000.0)
