@@ -46,14 +46,14 @@ UNIT = "accepted steps/s"
 FLOPS_PER_ACCEPTED_STEP = 6 * 446 + 275 + 6 * 23 + 4
 # FP32-pipe thread instructions (FFMA + FADD + FMUL) per accepted step of the
 # FP32-form guiding-centre kernel k_gc32 in the double dipole: the float-float
-# stages, field samples and equations, from one ncu capture (sm__sass_thread_
-# inst_executed_op_{ffma,fadd,fmul}_pred_on.sum over the launch's accepted
-# steps; profiles/k_gc32_doubledipole_262k_full.md).
-FP32_OPS_PER_ACCEPTED_STEP = 24000
+# stages, field samples and equations, from one ncu capture of the 262,144-
+# tracer case (sm__sass_thread_inst_executed_op_{ffma,fadd,fmul}_pred_on.sum
+# over the launch's accepted steps; profiles/k_gc32_doubledipole_262k_full.md).
+FP32_OPS_PER_ACCEPTED_STEP = 27970
 # DRAM traffic of one k_gc32 launch per tracer and simulated second
-# (dram__bytes_read.sum + dram__bytes_write.sum of the same capture, local-memory
+# (dram__bytes_read.sum + dram__bytes_write.sum of the same capture: local-memory
 # traffic; the algorithmic state traffic is ~464 B per tracer and launch).
-TRAFFIC_PER_TRACER_SECOND = 1.0e6
+TRAFFIC_PER_TRACER_SECOND = 6.14e5
 # FP64 FMA issue rate of a GB300 SM (thread-instructions per clock; ncu's FP64
 # pipe peak, 304 per clock over the 152 SMs).
 FP64_FMA_PER_CLK_PER_SM = 2
@@ -65,7 +65,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=1 << 20, help="tracers per GPU")
+    ap.add_argument("--n", type=int, default=None,
+                    help="tracers per GPU (default: 2^20 for the headline workload, the workload's own size otherwise)")
     ap.add_argument("--bc-delta", type=float, default=2.0, help="bc_drift_65k: BounceCenter.advance(delta) per step")
     ap.add_argument("--cpu-sample", type=int, default=0, help="tracers in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -237,14 +238,14 @@ def train_step_model(ctx, every=None):
     """Trains the step MLP on guiding centres drawn from the config-2
     distributions (8,192 electrons, an independent draw from the benchmark's):
     plain-controller samples then three on-policy rounds, 10 s each; then the
-    proposal scale is calibrated on the global error of 1,024 other config-2
+    proposal scale is calibrated on the global error of 2,048 other config-2
     electrons over 10 s (learned.calibrate_global). Deterministic."""
     from rapt_gb300 import learned, workloads as W
     w = W.subsample(W.config2(), np.arange(0, 65536, 8))
     t = time.perf_counter()
     p, info = learned.fit_gc(w, 10.0, ctx=ctx, rounds=3, steps=3000, capacity=1 << 23, mask=7)
     ctx.mlp_set_params(p)
-    wc = W.subsample(W.config2(), np.arange(4, 65536, 64))
+    wc = W.subsample(W.config2(), np.arange(4, 65536, 32))
     scale, table = learned.calibrate_global(wc, 10.0, ctx=ctx, every=every or LEARNED_EVERY)
     info["scale_samples"] = info["scale"]
     info["calibration_global"] = table
@@ -274,6 +275,7 @@ def exact_positions(w, idx, horizon, ctx):
 
 def run_ours(args, rank, ws, dist):
     from rapt_gb300 import Ensemble, workloads as W, fields as F
+    args.n = args.n or (1 << 20)
     from rapt_gb300 import _native as N
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     ctx = N.Context(dev)
@@ -542,7 +544,7 @@ def run_forms_workload(args, rank, ws, dist):
     from rapt_gb300 import Ensemble, workloads as W, _native as N
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     ctx = N.Context(dev)
-    if args.n != (1 << 20):
+    if args.n:
         n = args.n
     else:
         n = (1 << 18) if args.workload == "earthdipole_particles" else (1 << 16)
@@ -640,7 +642,7 @@ def run_grid_workload(args, rank, ws, dist):
     from rapt_gb300 import Ensemble, workloads as W, _native as N
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     ctx = N.Context(dev)
-    n = args.n if args.n != (1 << 20) else (1 << 18)
+    n = args.n or (1 << 18)
     w = W.gc_grid(n, seed=rank)
     t_build = time.perf_counter()
     g = W.dipole_grid()
@@ -709,7 +711,7 @@ def run_dense_workload(args, rank, ws, dist):
     from rapt_gb300 import Ensemble, workloads as W, fields as F, _native as N
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     ctx = N.Context(dev)
-    n = args.n if args.n != (1 << 20) else (1 << 18)
+    n = args.n or (1 << 18)
     w = W.subsample(W.gc_bench(1 << 20, seed=rank), np.arange(0, 1 << 20, (1 << 20) // n)[:n])
     cadence, span = 0.01, 0.5
     # 50 rows per step, plus the 17 a dense-output step may cover
@@ -801,7 +803,7 @@ def run_bc_workload(args, rank, ws, dist):
     from rapt_gb300 import workloads as W, fields as F, _native as N
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     ctx = N.Context(dev)
-    n = args.n if args.n != (1 << 20) else (1 << 16)
+    n = args.n or (1 << 16)
     w = W.bc_drift(1 << 16, seed=rank)
     if n < (1 << 16):  # an evenly spaced subset of the 65,536
         w = W.subsample(w, np.arange(0, 1 << 16, (1 << 16) // n)[:n])

@@ -143,10 +143,23 @@ __device__ __forceinline__ void stencil_gradB_curlb_df(const FieldP& f, double t
 // dx/dt = c u / gamma, du/dt = q/(m c) E + (q/m) (u x B) / gamma.
 template <int M>
 struct ParticleRHSdf {
-  FieldP f;
+  // field parameters referenced in the kernel's parameter space (__grid_constant__)
+  const FieldP& f;
   DF qmc, qm, igam;  // q/(m c), q/m, 1/gamma frozen at the start of advance() (static fields)
   bool eq;
+  // The equations are one non-inlined function taking and returning the state
+  // by value: DOP853 calls them at 12 stages, and one copy keeps the kernel's
+  // hot code small.
+  struct DF6 {
+    DF v0, v1, v2, v3, v4, v5;
+  };
   __device__ __forceinline__ void operator()(double t, const DF* Y, DF* o) const {
+    const DF6 r = eval(t, DF6{Y[0], Y[1], Y[2], Y[3], Y[4], Y[5]});
+    o[0] = r.v0; o[1] = r.v1; o[2] = r.v2; o[3] = r.v3; o[4] = r.v4; o[5] = r.v5;
+  }
+  __device__ __noinline__ DF6 eval(double t, DF6 Yv) const {
+    const DF Y[6] = {Yv.v0, Yv.v1, Yv.v2, Yv.v3, Yv.v4, Yv.v5};
+    DF o[6];
     DF ig = igam;
     if (!field_static<M>(f)) ig = df_rsqrt(DF{1.f, 0.f} + Y[3] * Y[3] + Y[4] * Y[4] + Y[5] * Y[5]);
     DF B[3], E[3];
@@ -159,6 +172,7 @@ struct ParticleRHSdf {
     o[4] = qmc * E[1] + a * (Y[5] * B[0] - Y[3] * B[2]);
     o[5] = qmc * E[2] + a * (Y[3] * B[1] - Y[4] * B[0]);
     if (eq) { o[2] = DF{0.f, 0.f}; o[5] = DF{0.f, 0.f}; }
+    return DF6{o[0], o[1], o[2], o[3], o[4], o[5]};
   }
 };
 

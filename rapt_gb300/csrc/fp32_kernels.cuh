@@ -11,7 +11,8 @@ namespace rapt {
 
 template <int M>
 // 4 blocks per SM: measured best for the 12-stage DOP853 float-float kernel.
-__global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, KParams P, Scratch* S) {
+__global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, const __grid_constant__ KParams P,
+                                                       Scratch* S) {
   int64_t idx = -1;
   bool exhausted = false;
   long long budget = P.budget;
@@ -334,7 +335,7 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
   for (;;) {
     warp_refill(&S->queue[1], E, RAPT_MODE_GC, idx, exhausted, load);
     if (__all_sync(kFull, idx < 0)) break;
-    lr.infer(P);
+    lr.infer(P, h);
     if (idx < 0) continue;
 
     const GcRHSdf<M> rhs{P.f, kmu, mcq, muq, qmc, P.enforce_eq != 0};

@@ -264,21 +264,24 @@ struct StepLearner {
   }
   float c_mass, c_energy, c_sign, c_pitch;  // per-tracer feature constants
   float rlast;                              // this lane's latest correction from the network (1: none yet)
+  float rcap;                               // cap on the correction of the pending step
   unsigned wit;                             // loop iterations of the warp (warp-uniform)
+  double hctl;                              // learned: the controller's proposal for the pending step
+  bool pend_apply;                          // learned: the pending step came from the staged accept
   double hbase;                             // collect: the controller's step after the sampled step
   double hcont;                             // learned: the step wanted before the interval-end clip
   bool want, pend, pend_sw, have_prop;
   uint32_t* sm;
 
   __device__ __forceinline__ void init(const KParams& P) {
-    want = pend = pend_sw = have_prop = false;
+    want = pend = pend_sw = have_prop = pend_apply = false;
     rlast = 1.f;
     wit = 0;
     sm = LRN ? rapt_dyn_smem + (threadIdx.x >> 5) * warp_words(P.collect != 0) : nullptr;
   }
   // Per-tracer constants; vs is the speed, pitch scale converts ppar to cos(pitch).
   __device__ __forceinline__ void load(double mass, double charge, double vs, double ppar_unit) {
-    want = pend = pend_sw = have_prop = false;
+    want = pend = pend_sw = have_prop = pend_apply = false;
     rlast = 1.f;
     if constexpr (LRN != 0) {
       const double gam = 1.0 / sqrt(1.0 - (vs / kC) * (vs / kC));
@@ -321,10 +324,13 @@ struct StepLearner {
              (mix64((uint64_t)idx * 0x100000001b3ull + (uint64_t)nacc) & P.samp_mask) == 0;
     }
     const bool inf = LRN == 2 && allow && !last;
+    const double hprop = hnew;  // the controller's proposal
     if constexpr (LRN == 2) {
       if (inf) {
         float cap = (float)(hmax / fabs(hnew));
         if (rej_before) cap = fminf(cap, (float)(fabs(h) / fabs(hnew)));
+        hctl = hnew;
+        rcap = cap;
         hnew *= (double)fminf(rlast, cap);
       }
     }
@@ -354,17 +360,19 @@ struct StepLearner {
       for (int i = 0; i < 16; ++i) row[i] = f[i];
       pend = coll;
       pend_sw = coll_sw;
-      hbase = hnew;
+      hbase = hprop;
     }
     if constexpr (LRN == 2) {
       if (inf) {
         stage_features(P.mlp_p, f, sm, lane);
         want = true;
+        pend_apply = true;
       }
     }
   }
   // Collect: label the staged sample with the attempt that followed it.
   __device__ __forceinline__ void on_attempt(const KParams& P, double h, double err, bool clipped) {
+    if constexpr (LRN == 2) pend_apply = false;  // the pending step has been attempted
     if constexpr (LRN != 0) {
       if (!pend) return;
       pend = false;
@@ -400,18 +408,23 @@ struct StepLearner {
     }
   }
   // Learned: warp-collective inference, on every learn_every-th iteration of
-  // the warp's loop, for the lanes that staged features since the last call;
-  // refreshes their correction (used from their next accepted step on). One
-  // call serves every lane that accepted a step in between, so its cost is
-  // spread over learn_every iterations. Called by all 32 lanes at the top of
-  // the loop.
-  __device__ __forceinline__ void infer(const KParams& P) {
+  // the warp's loop, for the lanes that staged features since the last call.
+  // It refreshes their correction; a lane whose pending step is the one
+  // proposed at the accept that staged the features gets the fresh correction
+  // on that step at once (from the controller's proposal, so corrections do
+  // not compound), the others from their next accepted step on. One call
+  // serves every lane that accepted a step in between, so its cost is spread
+  // over learn_every iterations. Called by all 32 lanes at the top of the loop.
+  __device__ __forceinline__ void infer(const KParams& P, double& h) {
     if constexpr (LRN == 2) {
       ++wit;
       if (wit % (unsigned)P.learn_every == 0u && __any_sync(kFull, want)) {
         float o[2];
         mlp_forward_staged(P.mlp_w, P.mlp_p, sm, o);
-        if (want) rlast = __expf(fminf(fmaxf(o[0], -3.f), 3.f)) * P.learn_scale;
+        if (want) {
+          rlast = __expf(fminf(fmaxf(o[0], -3.f), 3.f)) * P.learn_scale;
+          if (pend_apply) h = hctl * (double)fminf(rlast, rcap);
+        }
         want = false;
       }
     }

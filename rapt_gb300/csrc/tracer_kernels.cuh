@@ -618,7 +618,7 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
   for (;;) {
     warp_refill(&S->queue[1], E, RAPT_MODE_GC, idx, exhausted, load);
     if (__all_sync(kFull, idx < 0)) break;
-    lr.infer(P);
+    lr.infer(P, h);
     if (idx < 0) continue;
 
     const GcRHS<M> rhs{P.f, charge, qinv, mu, minv, kmu, inv_mc, igv, gmv, gmv2, P.gc_eom, P.enforce_eq != 0};
