@@ -224,7 +224,7 @@ def run_reference(args, rank, ws, dist):
 
 FORMS = (("plain", 0), ("fp32", 1), ("learned", 2), ("learned_fp32", 3))
 HEADLINE = "learned_fp32"
-LEARNED_EVERY = 1  # the network runs on every k-th step-loop iteration of a warp (rapt_config.learned_every)
+LEARNED_EVERY = 4  # the network runs on every k-th step-loop iteration of a warp (rapt_config.learned_every)
 
 
 def gyro_frequency_sum(w, magB):

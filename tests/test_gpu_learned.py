@@ -125,31 +125,40 @@ def trained(ctx):
 
 
 def test_learned_ab_against_plain(ctx, trained, oracle):
-    """Held-out (odd-indexed) tracers, 10 s: learned vs plain DOPRI5 control.
-    The learned form must need fewer right-hand-side evaluations per simulated
-    second, with a global error (against a tight-tolerance run) comparable to
-    the plain controller's."""
+    """Held-out (odd-indexed) tracers, 10 s: what the trained network gains over
+    the plain DOPRI5 controller, and at what price.
+
+    At the proposal scale calibrated on samples (the largest expected advance
+    per attempt) the network's proposals are far better predictions of the
+    largest acceptable step than the controller's (residual spread of log h*
+    a fraction of the controller's), so the learned form needs fewer
+    right-hand sides and rejects fewer steps -- but its steps sit nearer the
+    acceptance threshold and its global error (against a tight-tolerance run)
+    is larger than the plain controller's. At the scale calibrated on the
+    global error (learned.calibrate_global) the error is the plain
+    controller's or smaller, and the right-hand sides are not fewer: on these
+    orbits the trained proposals buy no work at matched accuracy."""
     w, p, info = trained
     print("fit", info)
     cal = info["calibration"][-1]
     assert info["losses"][0][-1][0] < 0.45, info  # below the mean predictor's 0.5
-    # on samples, the calibrated proposals advance further per attempt than the controller
-    assert cal["eff_learned"] > cal["eff_plain"], cal
+    # on samples, the calibrated proposals advance further per attempt than the
+    # controller, and predict the largest acceptable step more tightly
+    assert cal["eff_learned"] > cal["eff_plain"] and cal["resid_std"] < 0.5 * cal["target_std"], cal
     te = W.subsample(w, np.arange(1, len(w["mass"]), 2))
     ctx.mlp_set_params(p)
+    scale_g, table = learned.calibrate_global(W.subsample(w, np.arange(0, len(w["mass"]), 2)), 10.0, ctx=ctx)
+    assert scale_g is not None, table
+    runs = {"plain": (PLAIN, 1.0), "learned": (LEARNED, cal["scale"]), "learned_fp32": (LEARNED_FP32, cal["scale"]),
+            "matched": (LEARNED_FP32, scale_g)}
     res = {}
-    for form in (PLAIN, LEARNED, FP32, LEARNED_FP32):
-        e = gpu_ensemble(te, "gc", max_rows=16, form=form, learned_scale=cal["scale"])
+    for name, (form, scale) in runs.items():
+        e = gpu_ensemble(te, "gc", max_rows=16, form=form, learned_scale=scale)
         st = e.advance("gc", 10.0)
         h = e.download()
         bad = np.nonzero(h["status"])[0]
-        assert bad.size == 0, (form, st, np.unique(h["status"], return_counts=True), bad[:8],
-                               h["t_row"][bad[:8]], h["naccept"][bad[:8]], h["nreject"][bad[:8]])
-        res[form] = (st, h)
-    from tests._util import oracle_tracers
-    sel = np.arange(0, len(te["mass"]), 8)
-    f, cfg, tr = oracle_tracers(oracle, W.subsample(te, sel), "gc")
-    oracle.batch_advance(f, cfg, 1, tr, 10.0)
+        assert bad.size == 0, (name, st, np.unique(h["status"], return_counts=True), bad[:8])
+        res[name] = (st, h)
     # a tight-tolerance run as the exact solution: the global error of each form
     e = gpu_ensemble(te, "gc", max_rows=16, rtol=1e-12, atol=1e-12, nsteps=1000000)
     e.advance("gc", 10.0)
@@ -157,22 +166,23 @@ def test_learned_ab_against_plain(ctx, trained, oracle):
     assert np.all(he["status"] == 0)
     exact = he["s"]
     report = {}
-    for form, (st, h) in res.items():
-        pos, mom = rel_state_error(h["s"][:, sel], tr["s"], 4)
+    for name, (st, h) in res.items():
         gpos, _ = rel_state_error(h["s"], exact.T, 4)
-        report[form] = dict(acc=st["accepted"], rej=st["rejected"], rhs=st["rhs_evals"],
-                            rej_rate=st["rejected"] / max(st["accepted"], 1), pos_max=pos.max(),
-                            pos_med=float(np.median(pos)), glob_med=float(np.median(gpos)),
+        report[name] = dict(rhs=st["rhs_evals"], rej_rate=st["rejected"] / max(st["accepted"], 1),
+                            glob_med=float(np.median(gpos)), glob_p99=float(np.percentile(gpos, 99)),
                             glob_max=float(gpos.max()))
+    report["scale_samples"], report["scale_global"] = cal["scale"], scale_g
     print("A/B", report)
-    pl, le, lf = report[PLAIN], report[LEARNED], report[LEARNED_FP32]
-    # the gain: fewer right-hand sides per simulated second, fewer rejections
+    pl, le, lf, mt = report["plain"], report["learned"], report["learned_fp32"], report["matched"]
+    # the gain at the sample-calibrated scale: fewer right-hand sides and rejections
     assert le["rhs"] < 0.95 * pl["rhs"] and le["rej_rate"] < pl["rej_rate"], report
     assert abs(lf["rhs"] - le["rhs"]) < 0.01 * le["rhs"], report
-    # larger steps cost accuracy in proportion: global error (against a 1e-12
-    # run) within 3x of the plain controller's, per tracer at the median
-    for r in (le, lf):
-        assert r["glob_med"] < 3 * pl["glob_med"] and r["glob_max"] < 10 * pl["glob_max"], report
+    # ... bought with accuracy: a larger global error than the plain controller's
+    assert le["glob_med"] > pl["glob_med"], report
+    # at the globally calibrated scale: the plain controller's accuracy (up to
+    # the calibration sample's noise), and no saving of right-hand sides
+    assert mt["glob_p99"] <= 1.25 * pl["glob_p99"] and mt["glob_max"] <= 1.25 * pl["glob_max"], report
+    assert mt["rhs"] > 0.95 * pl["rhs"], report
 
 
 BENCH_HORIZON = 25  # bench.py's advance(1.0) count in the standard run: 5 warm-up + 20 timed steps
