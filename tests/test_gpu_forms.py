@@ -1,5 +1,5 @@
-"""The FP32 form (float-float stages, FP64 time / error norm / step control /
-guiding-centre stencil) against the CPU oracle and against the plain form."""
+"""The FP32 form (float-float stages and stencil differences, FP64 time / error
+norm / step size) against the CPU oracle and against the plain form."""
 import numpy as np
 import pytest
 
@@ -48,6 +48,27 @@ def test_fp32_particle_config4_sample():
     drift_gpu = np.abs(np.linalg.norm(h["s"][3:6].T, axis=1) / p0 - 1)
     drift_orc = np.abs(np.linalg.norm(tr["s"][:, 3:6], axis=1) / p0 - 1)
     assert np.median(drift_gpu) <= 2 * np.median(drift_orc) + 1e-12
+
+
+def test_fp32_adaptive_matches_plain():
+    """Adaptive in the Harris sheet (512 protons of config 3, a tenth of their
+    durations): the FP32 form's guiding-centre segments run float-float, its
+    particle segments the FP64 kernel (few, long and latency-bound); switch
+    counts, final modes and final positions follow the plain form's."""
+    w = W.subsample(W.config3(), np.arange(0, 262144, 512))
+    d = w["delta"] / 10
+    res = {}
+    for form in (0, FP32):
+        e = gpu_ensemble(w, "adaptive", max_rows=4096, max_switch=64, form=form)
+        st = e.advance("adaptive", d)
+        res[form] = (st, e.download())
+    (sa, ha), (sb, hb) = res[0], res[FP32]
+    assert np.all(ha["status"] == 0) and np.all(hb["status"] == 0)
+    assert abs(sb["switches"] - sa["switches"]) <= 0.02 * sa["switches"] + 2, (sa["switches"], sb["switches"])
+    same = ha["mode"] == hb["mode"]
+    assert same.mean() >= 0.95, same.mean()
+    pos = np.linalg.norm(ha["s"][:3] - hb["s"][:3], axis=0) / np.linalg.norm(ha["s"][:3], axis=0)
+    assert np.median(pos[same]) < 1e-6, np.median(pos[same])
 
 
 def oracle_mod():
