@@ -689,14 +689,7 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
   if (c->cfg.collect && !c->samp)
     return fail(c, RAPT_ERR_STATE, "collection without a sample buffer (rapt_mlp_samples_reserve)");
   // the step learner drives the guiding-centre kernels; particles run the plain controller
-  // Adaptive runs take their particle segments through the FP64 kernel in every
-  // form: those segments are few and long (a tracer that stays non-adiabatic
-  // steps on serially), so their time is the latency of one thread's dependent
-  // arithmetic, where a float-float operation is several FP32 instructions deep
-  // and slower than the FP64 one (config 5: FP32 particle segments made the
-  // whole run 0.78x the plain form's)
-  const bool f32p = f32 && kind == RAPT_KIND_PARTICLE;
-  int bps_p = f32p ? T.occ_particle32(block) : T.occ_particle[tab](block);
+  int bps_p = f32 ? T.occ_particle32(block) : T.occ_particle[tab](block);
   const bool dense = c->cfg.dense_output != 0;
   if (dense && kind != RAPT_KIND_PARTICLE && c->max_rows < 18)
     return fail(c, RAPT_ERR_INVALID, "dense output needs max_rows >= 18 (a step may cover 17 output times)");
@@ -749,7 +742,7 @@ static int advance_impl(Ctx* c, int kind, const double* delta, double delta_all,
     LaunchArgs a{Ev, P, c->scratch, 0, blk, s};
     if (kind != RAPT_KIND_GC) {
       a.grid = grid_p;
-      CK(f32p ? T.particle32(a) : T.particle[tab](a));
+      CK(f32 ? T.particle32(a) : T.particle[tab](a));
       ++kl;
     }
     if (kind != RAPT_KIND_PARTICLE) {

@@ -52,9 +52,9 @@ def test_fp32_particle_config4_sample():
 
 def test_fp32_adaptive_matches_plain():
     """Adaptive in the Harris sheet (512 protons of config 3, a tenth of their
-    durations): the FP32 form's guiding-centre segments run float-float, its
-    particle segments the FP64 kernel (few, long and latency-bound); switch
-    counts, final modes and final positions follow the plain form's."""
+    durations): the FP32 form (float-float particle and guiding-centre
+    segments) against the plain form -- switch counts, final modes and final
+    positions follow the plain form's."""
     w = W.subsample(W.config3(), np.arange(0, 262144, 512))
     d = w["delta"] / 10
     res = {}
