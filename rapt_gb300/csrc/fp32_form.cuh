@@ -228,24 +228,37 @@ struct GcRHSdf {
 #pragma unroll
       for (int i = 0; i < 3; ++i) { gB[i] = (float)gBd[i]; cb[i] = (float)cbd[i]; db[i] = (float)dbd[i]; }
     }
-    DF E[3];
-    FieldDF<M>::E(f, t, Y, E);
     const DF rg = df_rsqrt(DF{1.f, 0.f} + kmu * Bmag + u * u);
     const DF pq = mcq * u;  // ppar / q
-    DF Bs[3], Es[3];
     const DF mg = muq * rg;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      Bs[i] = B[i] + pq * cb[i];
-      if constexpr (FieldDF<M>::kDF) Es[i] = E[i] - mg * gB[i];  // static: db/dt = 0
-      else Es[i] = E[i] - (pq * db[i] + mg * gB[i]);
-    }
-    const DF iBsp = df_rcp(Bs[0] * ub[0] + Bs[1] * ub[1] + Bs[2] * ub[2]);
-    const DF Exb[3] = {Es[1] * ub[2] - Es[2] * ub[1], Es[2] * ub[0] - Es[0] * ub[2], Es[0] * ub[1] - Es[1] * ub[0]};
     const DF a = (u * rg) * DF(DFc(kC));
+    DF Bs[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) o[i] = (a * Bs[i] + Exb[i]) * iBsp;
-    o[3] = qmc * (Es[0] * Bs[0] + Es[1] * Bs[1] + Es[2] * Bs[2]) * iBsp;
+    for (int i = 0; i < 3; ++i) Bs[i] = B[i] + pq * cb[i];
+    const DF iBsp = df_rcp(Bs[0] * ub[0] + Bs[1] * ub[1] + Bs[2] * ub[2]);
+    if constexpr (FieldDF<M>::kDF) {
+      // static field, no E: E* = -(mu / (gamma q)) grad|B| carries the FP32
+      // quotient of the stencil, so E*, E* x b and E* . B* are FP32 (the drift
+      // is ~1e-4 of the velocity: its FP32 rounding is ~1e-11 of a slope)
+      const float mgf = df_f(mg);
+      const float Es[3] = {-mgf * gB[0], -mgf * gB[1], -mgf * gB[2]};
+      const float u0 = df_f(ub[0]), u1 = df_f(ub[1]), u2 = df_f(ub[2]);
+      const float Exb[3] = {Es[1] * u2 - Es[2] * u1, Es[2] * u0 - Es[0] * u2, Es[0] * u1 - Es[1] * u0};
+#pragma unroll
+      for (int i = 0; i < 3; ++i) o[i] = (a * Bs[i] + Exb[i]) * iBsp;
+      const float EsBs = Es[0] * df_f(Bs[0]) + Es[1] * df_f(Bs[1]) + Es[2] * df_f(Bs[2]);
+      o[3] = (qmc * EsBs) * iBsp;
+    } else {
+      DF E[3], Es[3];
+      FieldDF<M>::E(f, t, Y, E);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) Es[i] = E[i] - (pq * db[i] + mg * gB[i]);
+      const DF Exb[3] = {Es[1] * ub[2] - Es[2] * ub[1], Es[2] * ub[0] - Es[0] * ub[2],
+                         Es[0] * ub[1] - Es[1] * ub[0]};
+#pragma unroll
+      for (int i = 0; i < 3; ++i) o[i] = (a * Bs[i] + Exb[i]) * iBsp;
+      o[3] = qmc * (Es[0] * Bs[0] + Es[1] * Bs[1] + Es[2] * Bs[2]) * iBsp;
+    }
     if (eq) { o[2] = DF{0.f, 0.f}; o[3] = DF{0.f, 0.f}; }
     return DF4{o[0], o[1], o[2], o[3]};
   }
