@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E,
         lr.on_accept(P, idx, nacc, hstep, err, errprev, h, hmax, was_last, rej_before, nst - nacc_int <= 8,
                      (flags & RAPT_FLAG_CHECK_ADIABATICITY) != 0,
                      y[0].hi, y[1].hi, y[2].hi,
-                     y[3].hi, vs, 1.0 - (xend - rt) / hmax);
+                     y[3].hi, vs, interval_progress(xend, rt, hmax));
       } else {
         hnew = h * (double)ctl.reject_factor(safe, facc1);
         reject = true;

@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_mlp_train(TrainArgs a) {
     // ---- forward
     float xn[16];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) xn[i] = valid ? (smp[i] - p[kOffXmu + i]) / p[kOffXsig + i] : 0.f;
+    for (int i = 0; i < 16; ++i) xn[i] = valid ? norm_feature(smp[i], p[kOffXmu + i], p[kOffXsig + i]) : 0.f;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const uint32_t u = pack_bf16x2(xn[2 * i], xn[2 * i + 1]);

@@ -143,12 +143,17 @@ __device__ __forceinline__ void dense_out(const uint32_t* in, const uint32_t* WT
   y[1] = hi_t ? (hi_r ? v[1][3] : v[1][1]) : (hi_r ? v[0][3] : v[0][1]);
 }
 
+// One normalised feature, (v - mu) / sig, with the approximate FP32 quotient
+// (__fdividef, 2 ulp): features enter the network in BF16 (8 bits), and
+// training and inference normalise with this same function.
+__device__ __forceinline__ float norm_feature(float v, float mu, float sig) { return __fdividef(v - mu, sig); }
+
 // Normalise 16 raw features and write them as BF16 row `lane` of X (u32 [32][8]).
 __device__ __forceinline__ void stage_features(const float* p, const float* f, uint32_t* X, int lane) {
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    const float a = (f[2 * i] - p[kOffXmu + 2 * i]) / p[kOffXsig + 2 * i];
-    const float b = (f[2 * i + 1] - p[kOffXmu + 2 * i + 1]) / p[kOffXsig + 2 * i + 1];
+    const float a = norm_feature(f[2 * i], p[kOffXmu + 2 * i], p[kOffXsig + 2 * i]);
+    const float b = norm_feature(f[2 * i + 1], p[kOffXmu + 2 * i + 1], p[kOffXsig + 2 * i + 1]);
     X[lane * 8 + i] = pack_bf16x2(a, b);
   }
 }
@@ -237,6 +242,12 @@ __device__ __forceinline__ void mlp_forward_staged(const uint32_t* __restrict__ 
   out[1] = y1 * p[kOffYsig + 1] + p[kOffYmu + 1];
 }
 
+// Fraction of the output interval [xend - hmax, xend] done at time rt (a
+// learner feature; FP32 quotient).
+__device__ __forceinline__ float interval_progress(double xend, double rt, double hmax) {
+  return 1.f - __fdividef((float)(xend - rt), (float)hmax);
+}
+
 __host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
   x += 0x9e3779b97f4a7c15ull;
   x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
@@ -309,7 +320,7 @@ struct StepLearner {
   __device__ __forceinline__ void on_accept(const KParams& P, int64_t idx, long long nacc, double h, double err,
                                             double errprev, double& hnew, double hmax, bool last, bool rej_before,
                                             bool allow, bool row_check, float x, float y, float z, float ppar,
-                                            double vs, double progress) {
+                                            double vs, float progress) {
     if constexpr (LRN == 0) return;
     bool coll = false, coll_sw = false;
     if (last) {
@@ -325,10 +336,15 @@ struct StepLearner {
     }
     const bool inf = LRN == 2 && allow && !last;
     const double hprop = hnew;  // the controller's proposal
+    // step ratios in FP32 (approximate quotients): they are features and caps
+    // of a correction factor, and an FP64 division costs ~10 instructions of
+    // the FP64 pipe (1/64 of the FP32 rate). A step capped at hmax to within
+    // FP32 rounding is still clipped to the interval end (hmax = the interval).
+    const float fh = (float)fabs(h), fhn = (float)fabs(hnew), fhmax = (float)hmax;
     if constexpr (LRN == 2) {
       if (inf) {
-        float cap = (float)(hmax / fabs(hnew));
-        if (rej_before) cap = fminf(cap, (float)(fabs(h) / fabs(hnew)));
+        float cap = __fdividef(fhmax, fhn);
+        if (rej_before) cap = fminf(cap, __fdividef(fh, fhn));
         hctl = hnew;
         rcap = cap;
         hnew *= (double)fminf(rlast, cap);
@@ -337,19 +353,20 @@ struct StepLearner {
     if (!coll && !coll_sw && !inf) return;
     float f[16];
     const float r = sqrtf(x * x + y * y + z * z);
-    f[0] = __logf((float)(fabs(h) * vs) / r);
+    const float ir = __fdividef(1.f, r);
+    f[0] = __logf((float)(fabs(h) * vs) * ir);
     f[1] = __log10f(fmaxf((float)err, 1e-10f));
     f[2] = __log10f(fmaxf((float)errprev, 1e-10f));
-    f[3] = __logf((float)fabs(hnew / h));
+    f[3] = __logf(__fdividef(fhn, fh));
     f[4] = 1.f;
     f[5] = c_sign;
     f[6] = c_mass;
     f[7] = c_energy;
     f[8] = ppar * c_pitch;
     f[9] = __logf(r * (float)(1.0 / kRe));
-    f[10] = z / r;
-    f[11] = (float)progress;
-    f[12] = (float)(hmax / fabs(h));
+    f[10] = z * ir;
+    f[11] = progress;
+    f[12] = __fdividef(fhmax, fh);
     f[13] = rej_before ? 1.f : 0.f;
     f[14] = 0.f;
     f[15] = 0.f;

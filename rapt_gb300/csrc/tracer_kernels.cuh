@@ -728,7 +728,7 @@ __global__ void __launch_bounds__(128) k_gc(DevEnsemble E, KParams P, Scratch* S
           lr.on_accept(P, idx, nacc, hstep, err, errprev, h, hmax, was_last, rej_before, nst - nacc_int <= 8,
                      (flags & RAPT_FLAG_CHECK_ADIABATICITY) != 0,
                      (float)y[0], (float)y[1],
-                       (float)y[2], (float)y[3], vs, 1.0 - (xend - rt) / hmax);
+                       (float)y[2], (float)y[3], vs, interval_progress(xend, rt, hmax));
         } else {
           hnew = h / fmin(facc1, fac11 / safe);
           reject = true;
