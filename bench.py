@@ -45,15 +45,16 @@ UNIT = "accepted steps/s"
 # combination, error norm and control; rsqrt/sqrt/div/pow count as one flop each.
 FLOPS_PER_ACCEPTED_STEP = 6 * 446 + 275 + 6 * 23 + 4
 # FP32-pipe thread instructions (FFMA + FADD + FMUL) per accepted step of the
-# FP32-form guiding-centre kernel k_gc32 in the double dipole: the float-float
-# stages, field samples and equations, from one ncu capture of the 262,144-
-# tracer case (sm__sass_thread_inst_executed_op_{ffma,fadd,fmul}_pred_on.sum
-# over the launch's accepted steps; profiles/k_gc32_doubledipole_262k_full.md).
-FP32_OPS_PER_ACCEPTED_STEP = 27970
+# learned + FP32 guiding-centre kernel k_gc32<DoubleDipole, learned> (the
+# headline form): the float-float stages and centre field, the FP32 stencil
+# differences, the equations and the step learner, from one ncu capture of the
+# 262,144-tracer case (sm__sass_thread_inst_executed_op_{ffma,fadd,fmul}_pred_on.sum
+# over the launch's accepted steps; profiles/k_gc32_learned_doubledipole_262k_full.md).
+FP32_OPS_PER_ACCEPTED_STEP = 9947
 # DRAM traffic of one k_gc32 launch per tracer and simulated second
 # (dram__bytes_read.sum + dram__bytes_write.sum of the same capture: local-memory
 # traffic; the algorithmic state traffic is ~464 B per tracer and launch).
-TRAFFIC_PER_TRACER_SECOND = 6.14e5
+TRAFFIC_PER_TRACER_SECOND = 8.44e5
 # FP64 FMA issue rate of a GB300 SM (thread-instructions per clock; ncu's FP64
 # pipe peak, 304 per clock over the 152 SMs).
 FP64_FMA_PER_CLK_PER_SM = 2
@@ -255,6 +256,16 @@ def train_step_model(ctx, every=None):
     return p, info
 
 
+def hbm_peak_gbs():
+    """Measured HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json),
+    else 6,800 GB/s, an earlier measurement of the same copy."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return 6800.0
+
+
 def pos_errors(pos, ref):
     e = np.linalg.norm(pos - ref, axis=1) / np.linalg.norm(ref, axis=1)
     return {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)), "max": float(e.max())}
@@ -274,6 +285,7 @@ def exact_positions(w, idx, horizon, ctx):
 
 
 def run_ours(args, rank, ws, dist):
+    import torch
     from rapt_gb300 import Ensemble, workloads as W, fields as F
     args.n = args.n or (1 << 20)
     from rapt_gb300 import _native as N
@@ -329,10 +341,12 @@ def run_ours(args, rank, ws, dist):
         for _ in range(args.warmup):
             ens.advance("gc", 1.0)
             ens.rows(reset=True)
-        # ---- device-resident timed region
+        # ---- device-resident timed region (a profiler range: ncu --profile-from-start off
+        # captures these launches only)
         barrier(dist)
         acc = rej = rhs = launches = 0
         dev_ms = 0.0
+        torch.cuda.cudart().cudaProfilerStart()
         for _ in range(args.steps):
             st = ens.advance("gc", 1.0)
             acc += st["accepted"]
@@ -341,6 +355,7 @@ def run_ours(args, rank, ws, dist):
             dev_ms += st["kernel_ms"]
             launches += st["kernel_launches"]
             ens.ctx.check(ens.ctx.L.rapt_rows_download(ens.ctx.h, None, None, None, None, None, 1), "reset rows")
+        torch.cuda.cudart().cudaProfilerStop()
         barrier(dist)
         if idx is not None:
             h = ens.download()
@@ -429,7 +444,8 @@ def run_ours(args, rank, ws, dist):
                             "peak_source": "measured in-run: FP32 FMA chains (rapt_measure_peaks)",
                             "traffic": traffic, "traffic_note": "DRAM bytes per launch (local memory), "
                             "scaled from a 262,144-tracer ncu capture",
-                            "traffic_frac_hbm": traffic / (headr["ms_per_step"] * 1e-3) / 6788.3e9,
+                            "traffic_frac_hbm": traffic / (headr["ms_per_step"] * 1e-3) / (hbm_peak_gbs() * 1e9),
+                            "hbm_peak": hbm_peak_gbs(),
                             "plain_kernel": roof_plain}
     else:
         line["roofline"] = dict(roof_plain)

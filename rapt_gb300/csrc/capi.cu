@@ -158,9 +158,22 @@ void finish_field(FieldP* f) {
     f->dh[i] = (float)k[i];
     f->dl[i] = (float)(k[i] - (double)f->dh[i]);
   }
-  f->gsh = (float)f->gradstep;
-  f->gsl = (float)(f->gradstep - (double)f->gsh);
-  f->inv2df = (float)f->inv2d;
+  // the FP32 form's dipole stencil (fp32_form.cuh): positions in units of
+  // L = 2^22 m, unit coefficient; c = -B0 (Re / L)^3 in both dipole models
+  if (f->model == RAPT_EARTH_DIPOLE || f->model == RAPT_DOUBLE_DIPOLE) {
+    const double L = 4194304.0;
+    auto split = [](double v, float& h, float& l) { h = (float)v; l = (float)(v - (double)h); };
+    f->sd = (float)(f->gradstep / L);
+    const double step = (double)f->sd * L;  // the realised step (m)
+    const double c = -p[0] * (kRe / L) * (kRe / L) * (kRe / L);
+    split(fabs(c), f->cah, f->cal);
+    split(fabs(c) / (2.0 * step), f->sgh, f->sgl);
+    split((c < 0 ? -1.0 : 1.0) / (2.0 * step), f->sch, f->scl);
+    if (f->model == RAPT_DOUBLE_DIPOLE) {
+      split(p[1], f->sxh, f->sxl);
+      split(p[2], f->skh, f->skl);
+    }
+  }
 }
 
 // trace points per direction of the bounce-period field-line trace; a thread's

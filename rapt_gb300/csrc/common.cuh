@@ -27,8 +27,11 @@ struct FieldP {
   double inv2d;       // 1 / (2 gradstep)
   double c0, c1, c2;  // model constants precomputed on the host
   float dh[4], dl[4]; // float-float model constants (hi, lo) for the FP32 form
-  float gsh, gsl;     // FP32 form: gradstep as float-float
-  float inv2df;       // FP32 form: 1 / (2 gradstep)
+  // FP32 form, dipole models in units of L = 2^22 m with B = c F(r): the stencil
+  // step d / L, the second dipole's position (m) and strength, |c|, and the
+  // quotients |c| / (2 d) and sign(c) / (2 d) of the realised step, as
+  // float-float (hi, lo) pairs
+  float sd, sxh, sxl, skh, skl, cah, cal, sgh, sgl, sch, scl;
   // RAPT_GRID: axes and [nt][nx][ny][nz][3] snapshots resident on the device
   const double *gt, *gx, *gy, *gz;
   const double *gB, *gE;  // gE null: zero electric field

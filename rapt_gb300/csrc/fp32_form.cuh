@@ -4,8 +4,10 @@
 // arithmetic: the state, the stage derivatives, the tableau coefficients, the
 // field at the stage point and the dominant terms of the equations of motion are
 // hi + lo pairs of floats (df.cuh), so stage values keep ~48 bits. FP64 hardware
-// is kept for time, the error norm, the step size, and -- for guiding centres --
-// the finite-difference grad|B|, curl b and db/dt (the plain form's stencil).
+// is kept for time, the error norm and the step size. The guiding centres'
+// finite-difference grad|B| and curl b are FP32 differences formed without
+// cancellation for the dipole models, and the plain form's FP64 stencil (with
+// db/dt) for the others.
 // The error estimate is therefore accurate enough for the reference's norm
 // (rtol 1e-8 with a scalar atol applied to near-zero components), and the
 // controller follows the plain form's rules; its step-size factor err^(1/q) is
@@ -87,55 +89,188 @@ struct FieldDF<RAPT_DOUBLE_DIPOLE> {
   }
 };
 
-// grad|B| and curl b by the reference's central differences (fields.py:155-200,
-// the 6-point stencil of stencil_gradB_curlb): the six field samples, their
-// magnitudes and unit vectors in float-float (about 48 bits) and the
-// differences of the samples in float-float (nearly exact for these nearby
-// values, so the cancellation that makes single-precision samples useless
-// loses nothing here); the difference quotients in FP32. Their consumer is the
-// FP32 drift term of the equations, and the stencil's own truncation error,
-// (gradstep / r)^2 = 4e-8 at 5 Re, is larger than FP32 rounding; an FP64
-// quotient would cost ~45 FP64 instructions per right-hand side on a pipe that
-// runs at 1/64 of the FP32 rate.
-// One stencil sample: |B| and the unit vector b at x, float-float. Not
-// inlined, so that the kernel holds one copy of the field code for all seven
-// samples of a right-hand side (the kernel runs at high occupancy and its
-// instruction cache is a limit); arguments and result pass by value, in
-// registers, not through local memory.
-struct DFSample {
-  DF mag, u0, u1, u2;
-};
-template <int M>
-__device__ __noinline__ DFSample stencil_sample_df(const FieldP& f, double t, DF x0, DF x1, DF x2) {
-  const DF x[3] = {x0, x1, x2};
-  DF b[3];
-  FieldDF<M>::B(f, t, x, b);
-  const DF s2 = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
-  const DF ib = df_rsqrt(s2);
-  return DFSample{s2 * ib, b[0] * ib, b[1] * ib, b[2] * ib};
+// The dipole models' field for the guiding-centre equations: one routine gives
+// the centre sample (|B| and b, float-float: the streaming term b v_par is the
+// dominant slope) and the reference's central differences grad|B| and curl b
+// (fields.py:111-131, 175-200): (|B|(x + d e_a) - |B|(x - d e_a)) / 2d and the
+// same differences of b.
+//
+// The differences are FP32 and formed without cancellation. Subtracting two
+// samples of |B| loses the digits they share (d / r is 2e-4 for the double
+// dipole, 2e-7 for the Earth dipole), which is why the reference needs FP64
+// samples. Here no step subtracts two samples. For each dipole term
+// F(r) = P(r) s(r), P = (3 rz rx, 3 rz ry, 2 rz^2 - rx^2 - ry^2), s = |r|^-5:
+//   s(r +- d e_A) = s0 (1 + g(x+-)),  x+- = (d^2 +- 2 r_A d) / |r|^2,
+//   g(x) = (1 + x)^(-5/2) - 1 by its series (the direct form for |x| > 1e-2),
+// so the sum and difference of the two samples of s come from g's even and odd
+// parts, each to FP32's relative rounding; P's exact difference and sum give
+//   2 (F+ - F-) = (P+ - P-)(s+ + s-) + (P+ + P-)(s+ - s-),
+//   2 (F+ + F-) = (P+ + P-)(s+ + s-) + (P+ - P-)(s+ - s-),
+// and then
+//   |F+| - |F-| = (F+ - F-) . (F+ + F-) / (|F+| + |F-|),
+//   f+ - f-     = (F+ - F-) / |F+| - F- (|F+| - |F-|) / (|F+| |F-|).
+// The quotients are the reference's, with the same step d. s0 = |r|^-5 and
+// |r|^2 come from the float-float centre sample, which computes them anyway
+// (their rounding would scale every difference the same way). No step is
+// biased: positions are scaled by a power of two (units of L = 2^22 m),
+// reciprocal square roots are Newton-refined and divisions correctly rounded,
+// and the constants (the model's coefficient, the second dipole's position and
+// strength, the quotient 1 / 2d) enter as float-float. What remains is FP32
+// rounding noise, ~1e-7 of the gradient, which averages out along a
+// trajectory where a systematic error would not.
+constexpr float kStencilLinv = 1.f / 4194304.f;  // 1 / L, L = 2^22 m
+
+// 1 / sqrt(u) to within rounding: rsqrtf and one Newton step whose residual
+// 1 - u y^2 is formed with an exact product.
+__device__ __forceinline__ float rsqrt_nr(float u) {
+  const float y = rsqrtf(u);
+  const float t = u * y;
+  const float tl = fmaf(u, y, -t);  // u y = t + tl
+  const float r = fmaf(-tl, y, fmaf(-t, y, 1.f));
+  return fmaf(0.5f * y, r, y);
 }
 
-template <int M>
-__device__ __forceinline__ void stencil_gradB_curlb_df(const FieldP& f, double t, const DF* Y, float* gB,
-                                                       float* cb) {
-  const DF d{f.gsh, f.gsl};
-  const float s = f.inv2df;
-  float c0 = 0.f, c1 = 0.f, c2 = 0.f;
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    DF xp[3] = {Y[0], Y[1], Y[2]}, xm[3] = {Y[0], Y[1], Y[2]};
-    xp[a] = Y[a] + d;
-    xm[a] = Y[a] - d;
-    const DFSample sp = stencil_sample_df<M>(f, t, xp[0], xp[1], xp[2]);
-    const DFSample sm = stencil_sample_df<M>(f, t, xm[0], xm[1], xm[2]);
-    gB[a] = df_f(sp.mag - sm.mag) * s;
-    const DF up[3] = {sp.u0, sp.u1, sp.u2}, um[3] = {sm.u0, sm.u1, sm.u2};
-    auto du = [&](int i) { return df_f(up[i] - um[i]); };
-    if (a == 0) { c1 -= du(2); c2 += du(1); }
-    if (a == 1) { c0 += du(2); c2 -= du(0); }
-    if (a == 2) { c0 -= du(1); c1 += du(0); }
+// (1 + x)^(-5/2) - 1 for |x| <= 1e-2: the binomial series to x^6 (truncation
+// below 1e-12 relative).
+__device__ __forceinline__ float g52(float x) {
+  float a = 15015.f / 1024.f;
+  a = fmaf(a, x, -3003.f / 256.f);
+  a = fmaf(a, x, 1155.f / 128.f);
+  a = fmaf(a, x, -105.f / 16.f);
+  a = fmaf(a, x, 35.f / 8.f);
+  a = fmaf(a, x, -2.5f);
+  return a * x;
+}
+
+// One dipole term at r +- d e_A: dF = 2 (F+ - F-), sF = 2 (F+ + F-); s0 = |r|^-5,
+// r2 = |r|^2, ir2 = 1 / r2 (each rounded once from the float-float centre).
+template <int A>
+__device__ __forceinline__ void dipole_pm(float rx, float ry, float rz, float d, float s0, float r2, float ir2,
+                                          float* dF, float* sF) {
+  const float ra = A == 0 ? rx : (A == 1 ? ry : rz);
+  const float a1 = 2.f * ra * d * ir2, a0 = d * d * ir2;
+  float ss, ds;  // s+ + s-, s+ - s-
+  if (fabsf(a1) <= 1e-2f) {
+    const float gp = g52(a0 + a1), gm = g52(a0 - a1);
+    ss = s0 * (2.f + (gp + gm));
+    ds = s0 * (gp - gm);
+  } else {  // within ~100 d of a dipole: s+ - s- = (ip - iq)(ip^4 + ip^3 iq + ... + iq^4)
+    const float w = fmaf(d, d, r2), e = 2.f * ra * d;
+    const float u = w + e, v = w - e;
+    const float ip = rsqrt_nr(u), iq = rsqrt_nr(v);
+    const float ip2 = ip * ip, iq2 = iq * iq, ab = ip * iq, s2 = ip2 + iq2;
+    ss = fmaf(ip2 * ip2, ip, iq2 * iq2 * iq);
+    ds = __fdiv_rn(-2.f * e * ab * fmaf(s2, s2 + ab, -ab * ab), fmaf(u, ip, v * iq));
   }
-  cb[0] = c0 * s; cb[1] = c1 * s; cb[2] = c2 * s;
+  const float q = 2.f * (2.f * rz * rz - rx * rx - ry * ry);
+  float dP[3], sP[3];
+  sP[0] = 6.f * rz * rx;
+  sP[1] = 6.f * rz * ry;
+  if (A == 0) { dP[0] = 6.f * rz * d; dP[1] = 0.f; dP[2] = -4.f * rx * d; sP[2] = q - 2.f * d * d; }
+  if (A == 1) { dP[0] = 0.f; dP[1] = 6.f * rz * d; dP[2] = -4.f * ry * d; sP[2] = q - 2.f * d * d; }
+  if (A == 2) { dP[0] = 6.f * rx * d; dP[1] = 6.f * ry * d; dP[2] = 8.f * rz * d; sP[2] = q + 4.f * d * d; }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    dF[i] = fmaf(dP[i], ss, sP[i] * ds);
+    sF[i] = fmaf(sP[i], ss, dP[i] * ds);
+  }
+}
+
+// The float-float centre of one dipole term at r (units of L): F(r) and, for the
+// stencil, s0 = |r|^-5, |r|^2 and 1 / |r|^2 rounded to FP32.
+struct DipoleCentre {
+  DF F0, F1, F2;
+  float s0, r2, ir2;
+};
+__device__ __forceinline__ DipoleCentre dipole_centre(DF rx, DF ry, DF rz) {
+  const DF x2 = rx * rx, y2 = ry * ry, z2 = rz * rz;
+  const DF r2 = x2 + y2 + z2;
+  const DF ip = df_rsqrt(r2), ip2 = ip * ip;
+  const DF s0 = (ip2 * ip2) * ip;
+  const DF tz = rz * 3.f;
+  const DF q = (z2 * 2.f) - x2 - y2;
+  return DipoleCentre{(tz * rx) * s0, (tz * ry) * s0, q * s0, df_f(s0), df_f(r2), df_f(ip2)};
+}
+
+struct DipoleSample {
+  DF mag, u0, u1, u2;  // |B| and b at the centre
+  float g0, g1, g2;    // grad|B|
+  float c0, c1, c2;    // curl b
+};
+
+// Differences along axis A of the field with unit coefficient (the sign and
+// size of the coefficient enter the quotients): dmag = |F+| - |F-|,
+// db = f+ - f- (f = F / |F|).
+template <int M, int A>
+__device__ __forceinline__ void dipole_axis(const FieldP& f, float x, float y, float z, float xb,
+                                            const DipoleCentre& ca, const DipoleCentre& cb, float& dmag,
+                                            float* db) {
+  float dF[3], sF[3];
+  dipole_pm<A>(x, y, z, f.sd, ca.s0, ca.r2, ca.ir2, dF, sF);
+  if constexpr (M == RAPT_DOUBLE_DIPOLE) {  // F(r) + k F(r - xb e_x)
+    float dG[3], sG[3];
+    dipole_pm<A>(xb, y, z, f.sd, cb.s0, cb.r2, cb.ir2, dG, sG);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      dF[i] = fmaf(f.skl, dG[i], fmaf(f.skh, dG[i], dF[i]));
+      sF[i] = fmaf(f.skl, sG[i], fmaf(f.skh, sG[i], sF[i]));
+    }
+  }
+  // with Fp = sF + dF = 4 F+ and Fm = sF - dF = 4 F-:
+  //   |F+| - |F-| = (dF . sF) / (|Fp| + |Fm|),
+  //   f+ - f-     = 2 dF / |Fp| - Fm 4 (|F+| - |F-|) / (|Fp| |Fm|)
+  float Fp[3], Fm[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) { Fp[i] = sF[i] + dF[i]; Fm[i] = sF[i] - dF[i]; }
+  const float np = fmaf(Fp[0], Fp[0], fmaf(Fp[1], Fp[1], Fp[2] * Fp[2]));
+  const float nm = fmaf(Fm[0], Fm[0], fmaf(Fm[1], Fm[1], Fm[2] * Fm[2]));
+  const float ip = rsqrt_nr(np), im = rsqrt_nr(nm);
+  dmag = __fdiv_rn(fmaf(dF[0], sF[0], fmaf(dF[1], sF[1], dF[2] * sF[2])), fmaf(np, ip, nm * im));
+  const float t = 4.f * dmag * ip * im;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) db[i] = fmaf(2.f * dF[i], ip, -Fm[i] * t);
+}
+
+// Not inlined: one copy of the field code per kernel (the kernel runs at high
+// occupancy and its instruction cache is a limit); arguments and result pass
+// by value, in registers.
+template <int M>
+__device__ __noinline__ DipoleSample dipole_sample(const FieldP& f, DF X0, DF X1, DF X2) {
+  const DF rx{X0.hi * kStencilLinv, X0.lo * kStencilLinv}, ry{X1.hi * kStencilLinv, X1.lo * kStencilLinv},
+      rz{X2.hi * kStencilLinv, X2.lo * kStencilLinv};
+  const DipoleCentre ca = dipole_centre(rx, ry, rz);
+  DF F[3] = {ca.F0, ca.F1, ca.F2};
+  DipoleCentre cb{};
+  float xb = 0.f;
+  if constexpr (M == RAPT_DOUBLE_DIPOLE) {
+    const DF d = X0 - DF{f.sxh, f.sxl};
+    const DF rxb{d.hi * kStencilLinv, d.lo * kStencilLinv};
+    cb = dipole_centre(rxb, ry, rz);
+    const DF k{f.skh, f.skl};
+    F[0] = F[0] + cb.F0 * k; F[1] = F[1] + cb.F1 * k; F[2] = F[2] + cb.F2 * k;
+    xb = rxb.hi;
+  }
+  // B = c F: |B| = |c| |F|, b = sign(c) F / |F|
+  const DF s2 = F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
+  const DF iF = df_rsqrt(s2);
+  const DF sc{f.sch < 0.f ? -1.f : 1.f, 0.f};
+  const DF ui = iF * sc;
+  DipoleSample o;
+  o.mag = (s2 * iF) * DF{f.cah, f.cal};
+  o.u0 = F[0] * ui; o.u1 = F[1] * ui; o.u2 = F[2] * ui;
+  float d0, d1, d2, b0[3], b1[3], b2[3];
+  dipole_axis<M, 0>(f, rx.hi, ry.hi, rz.hi, xb, ca, cb, d0, b0);
+  dipole_axis<M, 1>(f, rx.hi, ry.hi, rz.hi, xb, ca, cb, d1, b1);
+  dipole_axis<M, 2>(f, rx.hi, ry.hi, rz.hi, xb, ca, cb, d2, b2);
+  // quotients |c| / (2 d) and sign(c) / (2 d) as float-float products
+  auto qg = [&](float v) { return fmaf(v, f.sgl, v * f.sgh); };
+  auto qc = [&](float v) { return fmaf(v, f.scl, v * f.sch); };
+  o.g0 = qg(d0); o.g1 = qg(d1); o.g2 = qg(d2);
+  // curl b = (d bz/dy - d by/dz, d bx/dz - d bz/dx, d by/dx - d bx/dy)
+  o.c0 = qc(b1[2] - b2[1]);
+  o.c1 = qc(b2[0] - b0[2]);
+  o.c2 = qc(b0[1] - b1[0]);
+  return o;
 }
 
 // ---------------------------------------------------------------- right-hand sides
@@ -202,13 +337,16 @@ struct GcRHSdf {
     DF o[4];
     const DF u = Y[3];
     DF B[3], Bmag, ub[3];
+    float gB[3], cb[3], db[3] = {0.f, 0.f, 0.f};
     if constexpr (FieldDF<M>::kDF) {
-      // the centre through the stencil's sample routine (one copy of the field
-      // code in the kernel), B = |B| b
-      const DFSample c = stencil_sample_df<M>(f, t, Y[0], Y[1], Y[2]);
+      static_assert(!FieldDF<M>::kDF || Field<M>::kStatic, "float-float field models are static");
+      // centre (float-float) and stencil differences (FP32) in one call, B = |B| b
+      const DipoleSample c = dipole_sample<M>(f, Y[0], Y[1], Y[2]);
       Bmag = c.mag;
       ub[0] = c.u0; ub[1] = c.u1; ub[2] = c.u2;
       B[0] = ub[0] * Bmag; B[1] = ub[1] * Bmag; B[2] = ub[2] * Bmag;
+      gB[0] = c.g0; gB[1] = c.g1; gB[2] = c.g2;
+      cb[0] = c.c0; cb[1] = c.c1; cb[2] = c.c2;
     } else {
       FieldDF<M>::B(f, t, Y, B);
       const DF b2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
@@ -216,11 +354,7 @@ struct GcRHSdf {
       Bmag = b2 * ib;
       ub[0] = B[0] * ib; ub[1] = B[1] * ib; ub[2] = B[2] * ib;
     }
-    float gB[3], cb[3], db[3] = {0.f, 0.f, 0.f};
-    if constexpr (FieldDF<M>::kDF) {
-      static_assert(!FieldDF<M>::kDF || Field<M>::kStatic, "float-float field models are static");
-      stencil_gradB_curlb_df<M>(f, t, Y, gB, cb);
-    } else {
+    if constexpr (!FieldDF<M>::kDF) {
       const double Xd[3] = {df_to_double(Y[0]), df_to_double(Y[1]), df_to_double(Y[2])};
       double gBd[3], cbd[3], dbd[3];
       stencil_gradB_curlb<M>(f, t, Xd, gBd, cbd);
@@ -291,8 +425,7 @@ static __constant__ DFpair kDp5Adf[7][6] = {
 // The same DOPRI5 attempt with the six right-hand sides in one rolled loop:
 // the right-hand side (float-float field, stencil and equations) is emitted
 // once instead of six times, which keeps the kernel inside the instruction
-// cache at the high occupancy this form runs at. The zero coefficients add
-// exact zeros.
+// cache at the high occupancy this form runs at.
 template <int NV, class F>
 __device__ __forceinline__ void dopri5_attempt_df_rolled(const F& f, double x, const DF* y, const DF* k1, double h,
                                                          const double* scale, double rtol, double atol, DF* y1,
@@ -305,11 +438,41 @@ __device__ __forceinline__ void dopri5_attempt_df_rolled(const F& f, double x, c
 #pragma unroll 1
   for (int s = 1; s <= 6; ++s) {
     const DFpair* A = kDp5Adf[s];
-    const DF a0{A[0].hi, A[0].lo}, a1{A[1].hi, A[1].lo}, a2{A[2].hi, A[2].lo}, a3{A[3].hi, A[3].lo},
-        a4{A[4].hi, A[4].lo}, a5{A[5].hi, A[5].lo};
+    DF acc[NV];
+    // only the slopes of row s (k1..k_s; the last row skips k2): warp-uniform
+    // tests, and the skipped terms would add exact zeros
+    {
+      const DF a{A[0].hi, A[0].lo};
 #pragma unroll
-    for (int i = 0; i < NV; ++i)
-      yt[i] = y[i] + hd * (k1[i] * a0 + k2[i] * a1 + k3[i] * a2 + k4[i] * a3 + k5[i] * a4 + k6[i] * a5);
+      for (int i = 0; i < NV; ++i) acc[i] = k1[i] * a;
+    }
+    if (s >= 2 && s <= 5) {
+      const DF a{A[1].hi, A[1].lo};
+#pragma unroll
+      for (int i = 0; i < NV; ++i) acc[i] = acc[i] + k2[i] * a;
+    }
+    if (s >= 3) {
+      const DF a{A[2].hi, A[2].lo};
+#pragma unroll
+      for (int i = 0; i < NV; ++i) acc[i] = acc[i] + k3[i] * a;
+    }
+    if (s >= 4) {
+      const DF a{A[3].hi, A[3].lo};
+#pragma unroll
+      for (int i = 0; i < NV; ++i) acc[i] = acc[i] + k4[i] * a;
+    }
+    if (s >= 5) {
+      const DF a{A[4].hi, A[4].lo};
+#pragma unroll
+      for (int i = 0; i < NV; ++i) acc[i] = acc[i] + k5[i] * a;
+    }
+    if (s == 6) {
+      const DF a{A[5].hi, A[5].lo};
+#pragma unroll
+      for (int i = 0; i < NV; ++i) acc[i] = acc[i] + k6[i] * a;
+    }
+#pragma unroll
+    for (int i = 0; i < NV; ++i) yt[i] = y[i] + hd * acc[i];
     f(x + kDp5C[s] * h, yt, kt);
 #pragma unroll
     for (int i = 0; i < NV; ++i) {

@@ -159,8 +159,9 @@ static __constant__ double kDp5C[7] = {0, dp5::c2, dp5::c3, dp5::c4, dp5::c5, 1.
 
 // The same DOPRI5 attempt with the six right-hand sides in one rolled loop, so
 // that an expensive right-hand side (the guiding-centre stencil) is emitted once
-// rather than six times; stage sums run over all earlier slopes with zero
-// coefficients where the tableau has none.
+// rather than six times. A stage sum takes only the slopes its tableau row uses
+// (row s uses k1..k_s, the last row all but k2): the tests on s are the same for
+// every lane of a warp, and the terms they skip would add exact zeros.
 template <int NV, class F, bool DENSE = false>
 __device__ __forceinline__ void dopri5_attempt_rolled(const F& f, double x, const double* y, const double* k1,
                                                       double h, double rtol, double atol, double* y1, double* k7,
@@ -172,9 +173,31 @@ __device__ __forceinline__ void dopri5_attempt_rolled(const F& f, double x, cons
 #pragma unroll 1
   for (int s = 1; s <= 6; ++s) {
     const double* A = kDp5A[s];
+    double acc[NV];
 #pragma unroll
-    for (int i = 0; i < NV; ++i)
-      yt[i] = y[i] + h * (A[0] * k1[i] + A[1] * k2[i] + A[2] * k3[i] + A[3] * k4[i] + A[4] * k5[i] + A[5] * k6[i]);
+    for (int i = 0; i < NV; ++i) acc[i] = A[0] * k1[i];
+    if (s >= 2 && s <= 5) {
+#pragma unroll
+      for (int i = 0; i < NV; ++i) acc[i] = fma(A[1], k2[i], acc[i]);
+    }
+    if (s >= 3) {
+#pragma unroll
+      for (int i = 0; i < NV; ++i) acc[i] = fma(A[2], k3[i], acc[i]);
+    }
+    if (s >= 4) {
+#pragma unroll
+      for (int i = 0; i < NV; ++i) acc[i] = fma(A[3], k4[i], acc[i]);
+    }
+    if (s >= 5) {
+#pragma unroll
+      for (int i = 0; i < NV; ++i) acc[i] = fma(A[4], k5[i], acc[i]);
+    }
+    if (s == 6) {
+#pragma unroll
+      for (int i = 0; i < NV; ++i) acc[i] = fma(A[5], k6[i], acc[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < NV; ++i) yt[i] = fma(h, acc[i], y[i]);
     f(x + kDp5C[s] * h, yt, kt);
 #pragma unroll
     for (int i = 0; i < NV; ++i) {

@@ -1,26 +1,40 @@
-"""The FP32 form (float-float stages and stencil differences, FP64 time / error
-norm / step size) against the CPU oracle and against the plain form."""
+"""The FP32 form (float-float stages, FP32 stencil differences without
+cancellation, FP64 time / error norm / step size) against the CPU oracle and
+against the plain form."""
 import numpy as np
 import pytest
 
 from rapt_gb300 import workloads as W
-from tests._util import gpu_ensemble, rel_state_error, sensitivity_envelope
+from tests._util import gpu_ensemble, oracle_config, oracle_tracers, rel_state_error, sensitivity_envelope
 
 pytestmark = pytest.mark.gpu
 FP32 = 1
 
 
 def test_fp32_gc_matches_oracle():
-    """Config 2 subsample, 10 s: relative position error <= 5e-6 (target 1e-6),
-    step counts within 1 % of the plain controller's."""
+    """Config 2 subsample (64 electrons), 10 s. The FP32 form takes the plain
+    controller's steps (step counts within 1 %) and differs from the FP64
+    oracle by rounding: the float-float stages and the FP32 stencil
+    differences (~1e-7 relative noise on grad|B| and curl b). Yardstick: the
+    oracle's own integration error against an rtol = atol = 1e-12 oracle run.
+    The FP32 form must stay far inside it (median and maximum below a tenth)
+    and be as accurate against the exact solution as the oracle itself."""
+    O = oracle_mod()
     w = W.subsample(W.config2(), np.arange(0, 65536, 1024))
-    tr, env_pos, _ = sensitivity_envelope(oracle_mod(), w, "gc", 10.0)
+    f, cfg, tr = oracle_tracers(O, w, "gc")
+    O.batch_advance(f, cfg, 1, tr, 10.0)
+    _, _, ex = oracle_tracers(O, w, "gc")
+    O.batch_advance(f, oracle_config(O, w, rtol=1e-12, atol=1e-12), 1, ex, 10.0)
     ens = gpu_ensemble(w, "gc", max_rows=16, form=FP32)
     ens.advance("gc", 10.0)
     h = ens.download()
     assert np.all(h["status"] == 0)
     pos, _ = rel_state_error(h["s"], tr["s"], 4)
-    assert pos.max() < 5e-6 and np.median(pos) < 1e-7, (pos.max(), np.median(pos))
+    own, _ = rel_state_error(tr["s"].T, ex["s"], 4)
+    vs_exact, _ = rel_state_error(h["s"], ex["s"], 4)
+    assert np.median(pos) < 0.1 * np.median(own) and pos.max() < 0.1 * own.max(), (pos, own)
+    assert np.median(pos) < 5e-7 and pos.max() < 5e-6, (np.median(pos), pos.max())
+    assert np.median(vs_exact) <= 1.05 * np.median(own) and vs_exact.max() <= 1.05 * own.max(), (vs_exact, own)
     dpp = np.abs(h["s"][3] - tr["s"][:, 3]) / (w["mass"] * W.c)
     assert dpp.max() < 1e-4, dpp.max()
     assert np.max(np.abs(h["naccept"] - tr["naccept"]) / tr["naccept"]) < 0.01
