@@ -242,14 +242,12 @@ __global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, const __gr
 
 template <int M, int LRN = 0>
 // LRN: 0 plain controller, 1 training-sample collection, 2 MLP step proposals.
-// 12 (plain controller) or 16 (MLP proposals) blocks of 128 threads per SM,
-// 40 or 32 registers with the rest spilled: the float-float stages are long
-// dependent FP32 chains, and on GB300 more resident warps hide their latency
-// better than registers avoid the spills. Measured on the 1M guiding-centre
-// step: 1 block/SM 1.11e8 accepted steps/s, 8: 4.41e8, 12: 4.53e8, 16: 4.27e8
-// (the MLP variant: 12: 3.45e8, 16: 3.50e8).
-__global__ void __launch_bounds__(128, LRN == 2 ? 16 : 12) k_gc32(DevEnsemble E, const __grid_constant__ KParams P,
-                                                                     Scratch* S) {
+// 8 blocks of 128 threads per SM, 64 registers: the balance between resident
+// warps (the float-float stages are long dependent FP32 chains) and the
+// local-memory traffic of spills. Measured on the 1M guiding-centre step
+// (FP32 / learned + FP32 accepted steps/s): 4 blocks/SM 1.44e9 / 1.04e9,
+// 6: 1.45e9 / 1.15e9, 8: 1.51e9 / 1.21e9, 12: 1.30e9 / 1.04e9, 16: 0.95e9 / 0.79e9.
+__global__ void __launch_bounds__(128, 8) k_gc32(DevEnsemble E, const __grid_constant__ KParams P, Scratch* S) {
   int64_t idx = -1;
   bool exhausted = false;
   long long budget = P.budget;
