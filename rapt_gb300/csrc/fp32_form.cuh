@@ -323,6 +323,9 @@ struct GcRHSdf {
   const FieldP& f;
   DF kmu, mcq, muq, qmc;  // 2 mu/(m c^2), m c/q, mu/q, q/(m c)
   bool eq;
+  // the stage time is read only by models without a float-float form (the dipole
+  // models are static); the others skip its FP64 arithmetic
+  static constexpr bool kTime = !FieldDF<M>::kDF;
   // The equations are one non-inlined function (one copy serves HINIT, the
   // first slope and the rolled stages) taking and returning the state by value.
   struct DF4 {
@@ -473,7 +476,7 @@ __device__ __forceinline__ void dopri5_attempt_df_rolled(const F& f, double x, c
     }
 #pragma unroll
     for (int i = 0; i < NV; ++i) yt[i] = y[i] + hd * acc[i];
-    f(x + kDp5C[s] * h, yt, kt);
+    f(F::kTime ? x + kDp5C[s] * h : x, yt, kt);
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
       if (s == 1) k2[i] = kt[i];
@@ -484,12 +487,20 @@ __device__ __forceinline__ void dopri5_attempt_df_rolled(const F& f, double x, c
       if (s == 6) { k7[i] = kt[i]; y1[i] = yt[i]; }
     }
   }
+  // error estimate sum_j e_j k_j = sum_{j > 1} e_j (k_j - k1) (the e_j sum to
+  // zero): the differences of nearby slopes are formed from the float-float
+  // parts (nearly exact where they cancel) and summed in FP32 -- the estimate
+  // is compared with the tolerance and needs a few digits, not 48 bits
   double e = 0.0;
 #pragma unroll
   for (int i = 0; i < NV; ++i) {
-    const DF ei = k1[i] * DF(DFc(e1)) + k3[i] * DF(DFc(e3)) + k4[i] * DF(DFc(e4)) + k5[i] * DF(DFc(e5)) +
-                  k6[i] * DF(DFc(e6)) + k7[i] * DF(DFc(e7));
-    const double r = err_ratio(df_to_double(ei) * (h * scale[i]), y[i], y1[i], scale[i], rtol, atol);
+    auto dk = [&](const DF& k) { return (k.hi - k1[i].hi) + (k.lo - k1[i].lo); };
+    float ei = (float)e3 * dk(k3[i]);
+    ei = fmaf((float)e4, dk(k4[i]), ei);
+    ei = fmaf((float)e5, dk(k5[i]), ei);
+    ei = fmaf((float)e6, dk(k6[i]), ei);
+    ei = fmaf((float)e7, dk(k7[i]), ei);
+    const double r = err_ratio((double)ei * (h * scale[i]), y[i], y1[i], scale[i], rtol, atol);
     e = fma(r, r, e);
   }
   err = sqrt_nr(e * (1.0 / NV));
