@@ -220,7 +220,8 @@ int rapt_field_eval(void* ctx, int what, int64_t n, const double* tpos, double* 
 
 /* Right-hand sides at given states for checks (Particle.py:284-298,
  * GuidingCenter.py:329-395). state[n][8] = (t, y0..y5, gm|mu), per-tracer
- * mass/charge/v; out[n][6]. */
+ * mass/charge/v; out[n][6]. With an FP32 form configured, the FP32 form's
+ * float-float equations (and its FP32 stencil differences) in SI units. */
 int rapt_rhs_eval(void* ctx, int mode, int64_t n, const double* state, const double* mass,
                   const double* charge, const double* v, double* out);
 

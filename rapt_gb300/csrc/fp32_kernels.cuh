@@ -10,8 +10,10 @@
 namespace rapt {
 
 template <int M>
-// 4 blocks per SM: measured best for the 12-stage DOP853 float-float kernel.
-__global__ void __launch_bounds__(128, 4) k_particle32(DevEnsemble E, const __grid_constant__ KParams P,
+// 2 blocks per SM (255 registers): measured best for the 12-stage DOP853
+// float-float kernel (config 4 at 262,144 particles: 2 blocks/SM 1.37e8 accepted
+// steps/s, 3: 1.26e8, 4: 1.18e8, 6: 1.05e8, 8: 1.02e8).
+__global__ void __launch_bounds__(128, 2) k_particle32(DevEnsemble E, const __grid_constant__ KParams P,
                                                        Scratch* S) {
   int64_t idx = -1;
   bool exhausted = false;
@@ -493,6 +495,37 @@ __global__ void __launch_bounds__(128, 8) k_gc32(DevEnsemble E, const __grid_con
     }
   }
   st.flush(S);
+}
+
+// Right-hand sides of the FP32 form at given states, for checks (rapt_rhs_eval
+// with an FP32 form configured): the float-float equations of k_particle32 and
+// k_gc32 (the Tao-Chan-Brizard equations; the FP32 forms run no other)
+// evaluated at the FP64 states and returned in SI units, state[n][8] = (t,
+// y0..y5, gm | mu), out[n][6] as k_rhs_eval.
+template <int M>
+__global__ void k_rhs_eval32(KParams P, int mode, int64_t n, const double* state, const double* mass,
+                             const double* charge, double* out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* s = state + 8 * i;
+  const double m = mass[i], q = charge[i], mc = m * kC;
+  double o[6] = {0, 0, 0, 0, 0, 0};
+  if (mode == 0) {
+    const DF Y[6] = {dfd(s[1]), dfd(s[2]), dfd(s[3]), dfd(s[4] / mc), dfd(s[5] / mc), dfd(s[6] / mc)};
+    const ParticleRHSdf<M> rhs{P.f, dfd(q / mc), dfd(q / m), dfd(m / s[7]), P.enforce_eq != 0};
+    DF d[6];
+    rhs(s[0], Y, d);
+    for (int k = 0; k < 6; ++k) o[k] = df_to_double(d[k]) * (k < 3 ? 1.0 : mc);
+  } else {
+    const double mu = s[7];
+    const DF Y[4] = {dfd(s[1]), dfd(s[2]), dfd(s[3]), dfd(s[4] / mc)};
+    const GcRHSdf<M> rhs{P.f, dfd(2.0 * mu / (m * kC * kC)), dfd(mc / q), dfd(mu / q), dfd(q / mc),
+                         P.enforce_eq != 0};
+    DF d[4];
+    rhs(s[0], Y, d);
+    for (int k = 0; k < 4; ++k) o[k] = df_to_double(d[k]) * (k < 3 ? 1.0 : mc);
+  }
+  for (int k = 0; k < 6; ++k) out[6 * i + k] = o[k];
 }
 
 }  // namespace rapt

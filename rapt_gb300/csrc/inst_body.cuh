@@ -99,7 +99,10 @@ cudaError_t field_eval(const FieldP& f, int what, int64_t n, const double* tpos,
 cudaError_t rhs_eval(const KParams& P, int mode, int64_t n, const double* state, const double* mass,
                      const double* charge, const double* v, double* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_rhs_eval<kM><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(P, mode, n, state, mass, charge, v, out);
+  if (P.form == RAPT_FORM_FP32 || P.form == RAPT_FORM_LEARNED_FP32)
+    k_rhs_eval32<kM><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(P, mode, n, state, mass, charge, out);
+  else
+    k_rhs_eval<kM><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(P, mode, n, state, mass, charge, v, out);
   return cudaGetLastError();
 }
 cudaError_t bounce_period(const FieldP& f, double flres, int64_t n, const double* in, double* out, double* scratch,

@@ -85,6 +85,63 @@ def test_fp32_adaptive_matches_plain():
     assert np.median(pos[same]) < 1e-6, np.median(pos[same])
 
 
+@pytest.mark.parametrize("name", ["DoubleDipole", "EarthDipole"])
+def test_fp32_rhs_matches_plain(ctx, name):
+    """The FP32 form's right-hand sides against the plain FP64 ones at random
+    states (L 3-8, |latitude| <= 45 deg). Guiding centres (Tao-Chan-Brizard):
+    the velocity to 1e-8 of the speed (the drifts, up to ~1e-2 of it for
+    10 MeV electrons, carry the FP32 stencil's ~1e-7 relative noise); the
+    mirror force dp_par/dt, whose grad|B| comes from the FP32 stencil
+    differences formed without cancellation, to 5e-6 of mu |grad B| / gamma and
+    without bias (mean relative difference below 1e-7). A stencil that took
+    the difference of two FP32 samples would be off by ~1e-3 of the gradient.
+    Particles: float-float throughout, 1e-12."""
+    from rapt_gb300 import fields as F
+    fld = getattr(F, name)()
+    fld.bind(ctx)
+    rng = np.random.default_rng(11)
+    n = 4096
+    L = rng.uniform(3, 8, n)
+    lat = rng.uniform(-np.pi / 4, np.pi / 4, n)
+    phi = rng.uniform(0, 2 * np.pi, n)
+    pos = (L * W.Re)[:, None] * np.column_stack([np.cos(lat) * np.cos(phi), np.cos(lat) * np.sin(phi),
+                                                 np.sin(lat)])
+    tp = np.column_stack([np.zeros(n), pos])
+    m, q = W.m_el, -W.e
+    ek = 10 ** rng.uniform(-1, 1, n) * W.MeV * W.e
+    gam = 1 + ek / (m * W.c ** 2)
+    v = W.c * np.sqrt(1 - 1 / gam ** 2)
+    p = gam * m * v
+    pa = np.radians(rng.uniform(15, 85, n))
+    magB = ctx.field_eval("magB", tp)[:, 0]
+    gB = np.linalg.norm(ctx.field_eval("gradB", tp)[:, :3], axis=1)
+    mu = (p * np.sin(pa)) ** 2 / (2 * m * magB)
+    ppar = p * np.cos(pa) * rng.choice([-1.0, 1.0], n)
+    st = np.column_stack([tp, ppar, np.zeros(n), np.zeros(n), mu])
+    try:
+        ctx.set_config(form=0)
+        ref = ctx.rhs_eval(1, st, m, q, v)
+        ctx.set_config(form=FP32)
+        got = ctx.rhs_eval(1, st, m, q, v)
+        dv = np.linalg.norm(got[:, :3] - ref[:, :3], axis=1) / v
+        assert dv.max() < 1e-8, (name, dv.max())
+        scale = mu * gB / gam
+        dp = (got[:, 3] - ref[:, 3]) / scale
+        assert np.abs(dp).max() < 5e-6 and abs(dp.mean()) < 1e-7, (name, np.abs(dp).max(), dp.mean())
+        # particles: the float-float Lorentz force
+        vel = rng.standard_normal((n, 3))
+        vel *= (v / np.linalg.norm(vel, axis=1))[:, None]
+        mom = (gam * m)[:, None] * vel
+        stp = np.column_stack([tp, mom, gam * m])
+        ctx.set_config(form=0)
+        refp = ctx.rhs_eval(0, stp, m, q)
+        ctx.set_config(form=FP32)
+        gotp = ctx.rhs_eval(0, stp, m, q)
+        assert np.allclose(gotp, refp, rtol=1e-12, atol=1e-12 * np.abs(refp).max(axis=0)), name
+    finally:
+        ctx.set_config()
+
+
 def oracle_mod():
     from oracle import oracle as O
     O.lib()
