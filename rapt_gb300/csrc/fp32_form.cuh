@@ -231,11 +231,11 @@ __device__ __forceinline__ void dipole_axis(const FieldP& f, float x, float y, f
   for (int i = 0; i < 3; ++i) db[i] = fmaf(2.f * dF[i], ip, -Fm[i] * t);
 }
 
-// Not inlined: one copy of the field code per kernel (the kernel runs at high
-// occupancy and its instruction cache is a limit); arguments and result pass
-// by value, in registers.
+// Inlined into the right-hand side, its one caller, which is not inlined: one
+// copy of the field code per kernel (the kernel's instruction fetch is a
+// limit), and no call of its own (measured 2 % faster than a separate call).
 template <int M>
-__device__ __noinline__ DipoleSample dipole_sample(const FieldP& f, DF X0, DF X1, DF X2) {
+__device__ __forceinline__ DipoleSample dipole_sample(const FieldP& f, DF X0, DF X1, DF X2) {
   const DF rx{X0.hi * kStencilLinv, X0.lo * kStencilLinv}, ry{X1.hi * kStencilLinv, X1.lo * kStencilLinv},
       rz{X2.hi * kStencilLinv, X2.lo * kStencilLinv};
   const DipoleCentre ca = dipole_centre(rx, ry, rz);
