@@ -130,15 +130,18 @@ __device__ __forceinline__ float rsqrt_approx_f32(float x) {
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
+// (The range tests are made on the FP32 value the seed needs anyway: FP32
+// compares leave the FP64 pipe alone.)
 __device__ __forceinline__ double rcp_nr(double x) {
-  const double ax = fabs(x);
-  if (!(ax > 1e-36 && ax < 1e36)) return 1.0 / x;
-  const double y = (double)rcp_approx_f32((float)x);
+  const float xf = (float)x;
+  if (!(fabsf(xf) > 1e-36f && fabsf(xf) < 1e36f)) return 1.0 / x;
+  const double y = (double)rcp_approx_f32(xf);
   return fma(y, fma(-x, y, 1.0), y);  // y (2 - x y)
 }
 __device__ __forceinline__ double sqrt_nr(double x) {
-  if (!(x > 1e-36 && x < 1e36)) return sqrt(x);
-  const double y = (double)rsqrt_approx_f32((float)x);
+  const float xf = (float)x;
+  if (!(xf > 1e-36f && xf < 1e36f)) return sqrt(x);
+  const double y = (double)rsqrt_approx_f32(xf);
   const double s = x * y;                   // sqrt(x) to 2^-23
   return fma(0.5 * y, fma(-s, s, x), s);    // s + (x - s^2) / (2 sqrt(x))
 }

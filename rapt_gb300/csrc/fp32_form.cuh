@@ -367,17 +367,21 @@ struct GcRHSdf {
     }
     const DF rg = df_rsqrt(DF{1.f, 0.f} + kmu * Bmag + u * u);
     const DF pq = mcq * u;  // ppar / q
-    const DF mg = muq * rg;
     const DF a = (u * rg) * DF(DFc(kC));
     DF Bs[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) Bs[i] = B[i] + pq * cb[i];
-    const DF iBsp = df_rcp(Bs[0] * ub[0] + Bs[1] * ub[1] + Bs[2] * ub[2]);
     if constexpr (FieldDF<M>::kDF) {
-      // static field, no E: E* = -(mu / (gamma q)) grad|B| carries the FP32
-      // quotient of the stencil, so E*, E* x b and E* . B* are FP32 (the drift
-      // is ~1e-4 of the velocity: its FP32 rounding is ~1e-11 of a slope)
-      const float mgf = df_f(mg);
+      // static field, no E. The curl-b term of B* (~rho / L of B) and E* =
+      // -(mu / (gamma q)) grad|B| carry the FP32 stencil's relative noise, so
+      // the curl-b term, E* x b and E* . B* are FP32 (the drift is ~1e-4..1e-2
+      // of the velocity; FP32 rounding of these terms is below the stencil's
+      // noise). The per-tracer constants q / (m c) and mu / q enter the mirror
+      // force through float-float products: rounded to FP32 they would bias
+      // every evaluation of a tracer the same way.
+      const float pqf = df_f(pq);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) Bs[i] = B[i] + pqf * cb[i];
+      const DF iBsp = df_rcp(Bs[0] * ub[0] + Bs[1] * ub[1] + Bs[2] * ub[2]);
+      const float mgf = df_f(muq * rg);
       const float Es[3] = {-mgf * gB[0], -mgf * gB[1], -mgf * gB[2]};
       const float u0 = df_f(ub[0]), u1 = df_f(ub[1]), u2 = df_f(ub[2]);
       const float Exb[3] = {Es[1] * u2 - Es[2] * u1, Es[2] * u0 - Es[0] * u2, Es[0] * u1 - Es[1] * u0};
@@ -386,6 +390,10 @@ struct GcRHSdf {
       const float EsBs = Es[0] * df_f(Bs[0]) + Es[1] * df_f(Bs[1]) + Es[2] * df_f(Bs[2]);
       o[3] = (qmc * EsBs) * iBsp;
     } else {
+      const DF mg = muq * rg;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) Bs[i] = B[i] + pq * cb[i];
+      const DF iBsp = df_rcp(Bs[0] * ub[0] + Bs[1] * ub[1] + Bs[2] * ub[2]);
       DF E[3], Es[3];
       FieldDF<M>::E(f, t, Y, E);
 #pragma unroll
