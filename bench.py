@@ -50,14 +50,14 @@ FLOPS_PER_ACCEPTED_STEP = 6 * 446 + 275 + 6 * 23 + 4
 # differences, the equations and the step learner, from one ncu capture of the
 # 262,144-tracer case (sm__sass_thread_inst_executed_op_{ffma,fadd,fmul}_pred_on.sum
 # over the launch's accepted steps; profiles/k_gc32_learned_doubledipole_262k_full.md).
-FP32_OPS_PER_ACCEPTED_STEP = 9644
+FP32_OPS_PER_ACCEPTED_STEP = 9575
 # DRAM traffic of one k_gc32 launch per tracer and simulated second
 # (dram__bytes_read.sum + dram__bytes_write.sum of the same capture: local-memory
 # traffic; the algorithmic state traffic is ~464 B per tracer and launch).
-TRAFFIC_PER_TRACER_SECOND = 1.480e5
+TRAFFIC_PER_TRACER_SECOND = 1.532e5
 # Pipe and issue utilisation of the same capture: the headline kernel saturates
 # neither pipe, and instruction fetch is its top stall (the bound it is on).
-HEADLINE_NCU = {"issue_active": 0.468, "fp32_pipe_active": 0.343, "fp64_pipe_active": 0.313,
+HEADLINE_NCU = {"issue_active": 0.482, "fp32_pipe_active": 0.354, "fp64_pipe_active": 0.303,
                 "top_stall": "no_instruction"}
 # FP64 FMA issue rate of a GB300 SM (thread-instructions per clock; ncu's FP64
 # pipe peak, 304 per clock over the 152 SMs).
