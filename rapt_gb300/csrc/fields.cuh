@@ -333,6 +333,115 @@ struct Field<RAPT_GRID> {
   }
 };
 
+// |B| and b from B, each product rounded on its own (values that feed a central
+// difference).
+__device__ __forceinline__ void unit_and_mag_of(const double* b, double* ub, double& mag) {
+  const double b2 = dot3(b, b);
+  const double ib = rsqrt(b2);
+  mag = __dmul_rn(b2, ib);
+  ub[0] = __dmul_rn(b[0], ib); ub[1] = __dmul_rn(b[1], ib); ub[2] = __dmul_rn(b[2], ib);
+}
+
+// One axis of a located point: the cell index and weight of v (ok: inside).
+struct GridAxis {
+  int i;
+  double w;
+  bool ok;
+};
+__device__ __forceinline__ GridAxis grid_axis(const double* __restrict__ g, int n, double inv, double v) {
+  GridAxis a{0, 0.0, grid_inside(g, n, v)};
+  if (a.ok) a.i = grid_cell(g, n, inv, v, a.w);
+  return a;
+}
+// The corner sum of K arrays at the point located by its four axes (NaN outside).
+template <int K>
+__device__ __forceinline__ void grid_sum_axes(const GridAxis& at, const GridAxis& ax, const GridAxis& ay,
+                                              const GridAxis& az, int nt, int nx, int ny, int nz,
+                                              const double* const* V, double* out) {
+  GridCell c;
+  c.ok = at.ok && ax.ok && ay.ok && az.ok;
+  if (!c.ok) {
+#pragma unroll
+    for (int k = 0; k < 3 * K; ++k) out[k] = __longlong_as_double(0x7ff8000000000000LL);
+    return;
+  }
+  c.sy = nz; c.sx = (int64_t)ny * nz; c.st = (int64_t)nx * c.sx;
+  c.ntc = nt > 1 ? 2 : 1;
+  c.wt = nt > 1 ? at.w : 1.0;
+  c.wx = ax.w; c.wy = ay.w; c.wz = az.w;
+  c.base = (nt > 1 ? at.i : 0) * c.st + ax.i * c.sx + ay.i * c.sy + az.i;
+  grid_sum<K>(c, V, out);
+}
+
+// Everything a guiding-centre right-hand side takes from a gridded field at one
+// point -- B and E, the reference's central differences grad|B| and curl b
+// (fields.py:111-131, 175-200) and db/dt (fields.py:225-245) -- from one cell
+// search. Each sample of the stencil differs from the centre in one
+// coordinate, so only that axis is searched again; the other axes keep the
+// centre's cell and weight, which are the values a full search of the sample
+// returns: every sample is the number a separate interpolation gives. Outside
+// the grid the values are NaN. Not inlined (one copy per kernel).
+struct GridFields {
+  double B[3], E[3], gB[3], cb[3], db[3];
+};
+static __device__ __noinline__ GridFields grid_gc_fields(RAPT_GRID_ARGS, const double* __restrict__ VB,
+                                                         const double* __restrict__ VE, double t, double x,
+                                                         double y, double z, double d, double inv2d, double ts,
+                                                         bool timedep) {
+  const GridAxis at = nt > 1 ? grid_axis(gt, nt, it_, t) : GridAxis{0, 1.0, true};
+  const GridAxis ax = grid_axis(gx, nx, ix_, x), ay = grid_axis(gy, ny, iy_, y), az = grid_axis(gz, nz, iz_, z);
+  GridFields r;
+  if (VE) {
+    const double* arr[2] = {VB, VE};
+    double o[6];
+    grid_sum_axes<2>(at, ax, ay, az, nt, nx, ny, nz, arr, o);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { r.B[k] = o[k]; r.E[k] = o[3 + k]; }
+  } else {
+    const double* arr[1] = {VB};
+    grid_sum_axes<1>(at, ax, ay, az, nt, nx, ny, nz, arr, r.B);
+    r.E[0] = r.E[1] = r.E[2] = 0.0;
+  }
+  const double* arr[1] = {VB};
+  const double X[3] = {x, y, z};
+  double c0 = 0.0, c1 = 0.0, c2 = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double* g = a == 0 ? gx : (a == 1 ? gy : gz);
+    const int n = a == 0 ? nx : (a == 1 ? ny : nz);
+    const double inv = a == 0 ? ix_ : (a == 1 ? iy_ : iz_);
+    double up[3], um[3], mp, mm, b[3];
+    {
+      const GridAxis s = grid_axis(g, n, inv, X[a] + d);
+      grid_sum_axes<1>(at, a == 0 ? s : ax, a == 1 ? s : ay, a == 2 ? s : az, nt, nx, ny, nz, arr, b);
+      unit_and_mag_of(b, up, mp);
+    }
+    {
+      const GridAxis s = grid_axis(g, n, inv, X[a] - d);
+      grid_sum_axes<1>(at, a == 0 ? s : ax, a == 1 ? s : ay, a == 2 ? s : az, nt, nx, ny, nz, arr, b);
+      unit_and_mag_of(b, um, mm);
+    }
+    r.gB[a] = (mp - mm) * inv2d;
+    if (a == 0) { c1 -= (up[2] - um[2]); c2 += (up[1] - um[1]); }
+    if (a == 1) { c0 += (up[2] - um[2]); c2 -= (up[0] - um[0]); }
+    if (a == 2) { c0 -= (up[1] - um[1]); c1 += (up[0] - um[0]); }
+  }
+  r.cb[0] = c0 * inv2d; r.cb[1] = c1 * inv2d; r.cb[2] = c2 * inv2d;
+  r.db[0] = r.db[1] = r.db[2] = 0.0;
+  if (timedep) {
+    double u1[3], u2[3], m1, m2, b[3];
+    const GridAxis t1 = nt > 1 ? grid_axis(gt, nt, it_, t - ts) : at;
+    grid_sum_axes<1>(t1, ax, ay, az, nt, nx, ny, nz, arr, b);
+    unit_and_mag_of(b, u1, m1);
+    const GridAxis t2 = nt > 1 ? grid_axis(gt, nt, it_, t + ts) : at;
+    grid_sum_axes<1>(t2, ax, ay, az, nt, nx, ny, nz, arr, b);
+    unit_and_mag_of(b, u2, m2);
+    const double sc = 0.5 / ts;
+    r.db[0] = (u2[0] - u1[0]) * sc; r.db[1] = (u2[1] - u1[1]) * sc; r.db[2] = (u2[2] - u1[2]) * sc;
+  }
+  return r;
+}
+
 // B and E at one point: one cell search for a Grid, the two model functions otherwise.
 template <int M>
 __device__ __forceinline__ void field_BE(const FieldP& f, double t, double x, double y, double z, double* B,
@@ -367,10 +476,7 @@ __device__ __forceinline__ void unit_and_mag(const FieldP& f, double t, double x
                                              double& mag) {
   double b[3];
   Field<M>::B(f, t, x, y, z, b);
-  const double b2 = dot3(b, b);
-  const double ib = rsqrt(b2);
-  mag = __dmul_rn(b2, ib);
-  ub[0] = __dmul_rn(b[0], ib); ub[1] = __dmul_rn(b[1], ib); ub[2] = __dmul_rn(b[2], ib);
+  unit_and_mag_of(b, ub, mag);
 }
 
 // The reference's central-difference stencil (fields.py:111-131 gradB and

@@ -341,6 +341,7 @@ struct GcRHSdf {
     const DF u = Y[3];
     DF B[3], Bmag, ub[3];
     float gB[3], cb[3], db[3] = {0.f, 0.f, 0.f};
+    DF Eg[3];  // Grid: E from the same cell search as B
     if constexpr (FieldDF<M>::kDF) {
       static_assert(!FieldDF<M>::kDF || Field<M>::kStatic, "float-float field models are static");
       // centre (float-float) and stencil differences (FP32) in one call, B = |B| b
@@ -351,13 +352,27 @@ struct GcRHSdf {
       gB[0] = c.g0; gB[1] = c.g1; gB[2] = c.g2;
       cb[0] = c.c0; cb[1] = c.c1; cb[2] = c.c2;
     } else {
-      FieldDF<M>::B(f, t, Y, B);
+      double Ed[3] = {0.0, 0.0, 0.0};
+      if constexpr (M == RAPT_GRID) {
+        // B, E, the stencil and db/dt of the plain form from one cell search
+        const GridFields g = grid_gc_fields(RAPT_GRID_PASS(f), f.gB, f.gE, t, df_to_double(Y[0]),
+                                            df_to_double(Y[1]), df_to_double(Y[2]), f.gradstep, f.inv2d,
+                                            f.timestep, !field_static<M>(f));
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          B[k] = dfd(g.B[k]); Ed[k] = g.E[k];
+          gB[k] = (float)g.gB[k]; cb[k] = (float)g.cb[k]; db[k] = (float)g.db[k];
+        }
+      } else {
+        FieldDF<M>::B(f, t, Y, B);
+      }
       const DF b2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
       const DF ib = df_rsqrt(b2);
       Bmag = b2 * ib;
       ub[0] = B[0] * ib; ub[1] = B[1] * ib; ub[2] = B[2] * ib;
+      if constexpr (M == RAPT_GRID) { Eg[0] = dfd(Ed[0]); Eg[1] = dfd(Ed[1]); Eg[2] = dfd(Ed[2]); }
     }
-    if constexpr (!FieldDF<M>::kDF) {
+    if constexpr (!FieldDF<M>::kDF && M != RAPT_GRID) {
       const double Xd[3] = {df_to_double(Y[0]), df_to_double(Y[1]), df_to_double(Y[2])};
       double gBd[3], cbd[3], dbd[3];
       stencil_gradB_curlb<M>(f, t, Xd, gBd, cbd);
@@ -395,7 +410,8 @@ struct GcRHSdf {
       for (int i = 0; i < 3; ++i) Bs[i] = B[i] + pq * cb[i];
       const DF iBsp = df_rcp(Bs[0] * ub[0] + Bs[1] * ub[1] + Bs[2] * ub[2]);
       DF E[3], Es[3];
-      FieldDF<M>::E(f, t, Y, E);
+      if constexpr (M == RAPT_GRID) { E[0] = Eg[0]; E[1] = Eg[1]; E[2] = Eg[2]; }
+      else FieldDF<M>::E(f, t, Y, E);
 #pragma unroll
       for (int i = 0; i < 3; ++i) Es[i] = E[i] - (pq * db[i] + mg * gB[i]);
       const DF Exb[3] = {Es[1] * ub[2] - Es[2] * ub[1], Es[2] * ub[0] - Es[0] * ub[2],

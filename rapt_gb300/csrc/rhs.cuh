@@ -46,10 +46,13 @@ struct GcRHS {
   __device__ __forceinline__ void operator()(double t, const double* Y, double* o) const {
     const double ppar = Y[3];
     double ub[3], Bmag;
-    double B[3], Eg[3];
-    if constexpr (M == RAPT_GRID) {  // one cell search for B and E
-      if (eom == 0) field_BE<M>(f, t, Y[0], Y[1], Y[2], B, Eg);
-      else Field<M>::B(f, t, Y[0], Y[1], Y[2], B);
+    double B[3], gB[3], cb[3], Eg[3], dbg[3];
+    if constexpr (M == RAPT_GRID) {
+      // B, E, the stencil and db/dt from one cell search (grid_gc_fields)
+      const GridFields g = grid_gc_fields(RAPT_GRID_PASS(f), f.gB, eom == 0 ? f.gE : nullptr, t, Y[0], Y[1], Y[2],
+                                          f.gradstep, f.inv2d, f.timestep, eom == 0 && !field_static<M>(f));
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { B[k] = g.B[k]; Eg[k] = g.E[k]; gB[k] = g.gB[k]; cb[k] = g.cb[k]; dbg[k] = g.db[k]; }
     } else {
       Field<M>::B(f, t, Y[0], Y[1], Y[2], B);
     }
@@ -59,16 +62,19 @@ struct GcRHS {
       Bmag = b2 * ib;
       ub[0] = B[0] * ib; ub[1] = B[1] * ib; ub[2] = B[2] * ib;
     }
-    double gB[3], cb[3];
-    stencil_gradB_curlb<M>(f, t, Y, gB, cb);
+    if constexpr (M != RAPT_GRID) stencil_gradB_curlb<M>(f, t, Y, gB, cb);
     if (eom == 0) {
       const double pm = ppar * inv_mc;
       const double g2 = 1.0 + k_mu * Bmag + pm * pm;
       const double rg = rsqrt(g2);
       double E[3], db[3];
-      if constexpr (M == RAPT_GRID) { E[0] = Eg[0]; E[1] = Eg[1]; E[2] = Eg[2]; }
-      else Field<M>::E(f, t, Y[0], Y[1], Y[2], E);
-      dbdt<M>(f, t, Y, db);
+      if constexpr (M == RAPT_GRID) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { E[k] = Eg[k]; db[k] = dbg[k]; }
+      } else {
+        Field<M>::E(f, t, Y[0], Y[1], Y[2], E);
+        dbdt<M>(f, t, Y, db);
+      }
       const double pq = ppar * qinv;
       double Bs[3] = {B[0] + pq * cb[0], B[1] + pq * cb[1], B[2] + pq * cb[2]};
       const double iBsp = 1.0 / dot3(Bs, ub);
