@@ -361,9 +361,14 @@ def run_ours(args, rank, ws, dist):
             ens.ctx.check(ens.ctx.L.rapt_rows_download(ens.ctx.h, None, None, None, None, None, 1), "reset rows")
         torch.cuda.cudart().cudaProfilerStop()
         barrier(dist)
+        # after the timed steps: tracers that ended with a failure status (RAPT_ST_*)
+        h = ens.download()
+        bad = h["status"] != 0
+        codes, counts = np.unique(h["status"][bad], return_counts=True)
+        failed = {"tracers": int(np.count_nonzero(bad)), "status": {int(c): int(k) for c, k in zip(codes, counts)},
+                  "first": [int(i) for i in np.flatnonzero(bad)[:4]]}
         if idx is not None:
-            h = ens.download()
-            finals[name] = (h["s"][:3, idx].T.copy(), int(np.count_nonzero(h["status"])))
+            finals[name] = (h["s"][:3, idx].T.copy(), failed)
         dev_s = allmax(dist, dev_ms * 1e-3)
         acc_all = allsum(dist, acc)
         sim = allsum(dist, float(n * args.steps))
@@ -372,7 +377,7 @@ def run_ours(args, rank, ws, dist):
                          "reject_rate": rej / max(acc, 1), "rhs_per_tracer_second": rhs / (n * args.steps),
                          "tracer_seconds_per_s": sim / dev_s,
                          "gyro_periods_per_s": allsum(dist, fgyro * args.steps) / dev_s,
-                         "kernel_launches": int(launches), "device_ms": dev_ms}
+                         "kernel_launches": int(launches), "device_ms": dev_ms, "failed": failed}
     wall = time.perf_counter() - t_all
     clocks = clk.stop() if clk else None
     headr = results[head]

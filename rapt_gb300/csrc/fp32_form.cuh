@@ -430,9 +430,11 @@ struct GcRHSdf {
 // form's norm on SI values: e_si is the FP64 error estimate; the scale's |y| is
 // taken from the float parts (a tolerance scale needs a few digits) and the
 // quotient is a Newton-refined reciprocal (rcp_nr, ~1e-14).
-__device__ __forceinline__ double err_ratio(double e_si, DF y0, DF y1, double scale, double rtol, double atol) {
+// floor: a lower bound of the tolerance (0: the plain form's norm).
+__device__ __forceinline__ double err_ratio(double e_si, DF y0, DF y1, double scale, double rtol, double atol,
+                                           double floor = 0.0) {
   const float ym = fmaxf(fabsf(y0.hi), fabsf(y1.hi));
-  return e_si * rcp_nr(fma(rtol * scale, (double)ym, atol));
+  return e_si * rcp_nr(fmax(fma(rtol * scale, (double)ym, atol), floor));
 }
 
 // The DOPRI5 tableau as float-float pairs in constant memory (rows as kDp5A).
@@ -514,7 +516,23 @@ __device__ __forceinline__ void dopri5_attempt_df_rolled(const F& f, double x, c
   // error estimate sum_j e_j k_j = sum_{j > 1} e_j (k_j - k1) (the e_j sum to
   // zero): the differences of nearby slopes are formed from the float-float
   // parts (nearly exact where they cancel) and summed in FP32 -- the estimate
-  // is compared with the tolerance and needs a few digits, not 48 bits
+  // is compared with the tolerance and needs a few digits, not 48 bits.
+  // Position components (0..2, metres): the tolerance is floored at 3e-9 of the
+  // step's displacement. The FP32 stencil differences put ~1e-7 relative noise
+  // on the drift velocity (at most a few per cent of the speed), which the slopes
+  // and so the estimate inherit: ~1e-9 of the displacement. Where the
+  // reference's scalar tolerance atol + rtol |x| is tighter than that -- a
+  // coordinate crossing zero slowly, where atol (1e-8 m) governs alone -- the
+  // controller would shrink the step chasing the noise until the interval
+  // exceeds nsteps. Elsewhere the floor (~5 mm on a 2e6 m step) is far below
+  // the tolerance (~0.3 m) and changes nothing.
+  float dp2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float d = (y1[i].hi - y[i].hi) + (y1[i].lo - y[i].lo);
+    dp2 = fmaf(d, d, dp2);
+  }
+  const double pfloor = 3e-9 * (double)sqrtf(dp2);
   double e = 0.0;
 #pragma unroll
   for (int i = 0; i < NV; ++i) {
@@ -524,7 +542,7 @@ __device__ __forceinline__ void dopri5_attempt_df_rolled(const F& f, double x, c
     ei = fmaf((float)e5, dk(k5[i]), ei);
     ei = fmaf((float)e6, dk(k6[i]), ei);
     ei = fmaf((float)e7, dk(k7[i]), ei);
-    const double r = err_ratio((double)ei * (h * scale[i]), y[i], y1[i], scale[i], rtol, atol);
+    const double r = err_ratio((double)ei * (h * scale[i]), y[i], y1[i], scale[i], rtol, atol, i < 3 ? pfloor : 0.0);
     e = fma(r, r, e);
   }
   err = sqrt_nr(e * (1.0 / NV));

@@ -11,8 +11,9 @@ namespace rapt {
 
 template <int M>
 // 2 blocks per SM (255 registers): measured best for the 12-stage DOP853
-// float-float kernel (config 4 at 262,144 particles: 2 blocks/SM 1.37e8 accepted
-// steps/s, 3: 1.26e8, 4: 1.18e8, 6: 1.05e8, 8: 1.02e8).
+// float-float kernel (262,144 protons and electrons in the Earth dipole, 50
+// gyro-periods each: 2 blocks/SM 1.37e8 accepted steps/s, 3: 1.26e8,
+// 4: 1.18e8, 6: 1.05e8, 8: 1.02e8).
 __global__ void __launch_bounds__(128, 2) k_particle32(DevEnsemble E, const __grid_constant__ KParams P,
                                                        Scratch* S) {
   int64_t idx = -1;
