@@ -7,7 +7,9 @@ quadratic spline of |B| between its brentq mirror points to convergence; the
 reference uses QUADPACK at epsrel 1e-4 and, for the second invariant below 70
 degrees equatorial pitch angle, a Simpson branch that raises NameError
 (flutils.py:130). ``usedipole=True`` uses the closed dipole forms of
-``rapt_gb300.utils``. ``criticalpoints`` (flutils.py:21-63) is not provided.
+``rapt_gb300.utils``. ``eye_error`` is the difference of the two.
+``criticalpoints`` (flutils.py:21-63) and ``fl_error`` (flutils.py:318-352),
+which need the traced points of a field line, are not provided.
 """
 import numpy as np
 
@@ -62,5 +64,16 @@ def gradI(tpos, field, Bm, usedipole=False):
     return out[0] if single else out
 
 
+def eye_error(tpos, field, Bm):
+    """flutils.eye_error (flutils.py:354-377): the second invariant from the
+    field line minus the closed dipole form."""
+    return eye(tpos, field, Bm, usedipole=False) - eye(tpos, field, Bm, usedipole=True)
+
+
 def criticalpoints(tpos, field, Bm):
     raise NotImplementedError("flutils.criticalpoints is not on the device path")
+
+
+def fl_error(tpos, field, Bm):
+    raise NotImplementedError("flutils.fl_error needs the traced field-line points, which the device path "
+                              "does not return")

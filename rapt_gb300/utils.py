@@ -164,3 +164,52 @@ def dipole_gradI(x, y, Bm, h):
     r0 = np.sqrt(x ** 2 + y ** 2)
     mag = (dipoleI(r0 + h, Bm) - dipoleI(r0 - h, Bm)) / (2 * h)
     return mag * np.array((x, y, 0)) / r0
+
+
+def Bm(tpos, pa, field):
+    """The mirror field |B| / sin^2(pa) at tpos for a pitch angle pa in degrees,
+    first invariant conserved (rapt/utils.py:516-522); |B| from the device."""
+    return field.magB(tpos) / np.sin(pa * np.pi / 180) ** 2
+
+
+def dipoleBm(L, eqpa):
+    """The mirror field B0 / L^3 / sin^2(eqpa) of the Earth dipole for the
+    equatorial distance L (Re) and equatorial pitch angle eqpa in degrees
+    (rapt/utils.py:524-529)."""
+    return B0 / L ** 3 / np.sin(eqpa * np.pi / 180) ** 2
+
+
+def dipole_bounce_period(L, v, eqpa):
+    """Bounce period (s) in the Earth dipole, Walt's approximation
+    0.117 L / beta (1 - 0.4635 sin(eqpa)^0.75) (M. Walt, Introduction to
+    Geomagnetically Trapped Radiation, p. 49; rapt/utils.py:489-513)."""
+    beta = v / c
+    return 0.117 * L / beta * (1 - 0.4635 * np.sin(eqpa * np.pi / 180) ** 0.75)
+
+
+def _walt_drift(k, L, v, eqpa):
+    beta = v / c
+    g = 1 / np.sqrt(1 - beta ** 2)
+    return k / (L * g * beta ** 2) * (1 - np.sin(eqpa * np.pi / 180) ** 0.62 / 3)
+
+
+def dipole_drift_period_p(L, v, eqpa):
+    """Proton drift period (s) in the Earth dipole, Walt's approximation
+    8.481 / (L gamma beta^2) (1 - sin(eqpa)^0.62 / 3) (Walt, p. 49;
+    rapt/utils.py:435-460)."""
+    return _walt_drift(8.481, L, v, eqpa)
+
+
+def dipole_drift_period_e(L, v, eqpa):
+    """Electron drift period (s) in the Earth dipole, Walt's approximation with
+    1.557e4 in place of the proton's 8.481 (rapt/utils.py:462-487)."""
+    return _walt_drift(1.557e4, L, v, eqpa)
+
+
+def drift_error(b):
+    """Relative deviation of each trajectory point of a BounceCenter from the
+    distance of its first point, (|r| - |r0|) / |r0| (a dipole's drift path is
+    a circle; rapt/utils.py:583-607)."""
+    r = np.sqrt(np.sum(b.trajectory[:, 1:] ** 2, axis=1))
+    return (r - r[0]) / r[0]
+

@@ -114,3 +114,20 @@ def test_flutils_facade(oracle):
     mid, x, y, z, Bm, gx, gy, gz = GOLD["gradI"][0]
     g = R.flutils.gradI(np.array([0.0, x, y, z]), fld, Bm)
     assert np.allclose(g, [gx, gy, gz], rtol=1e-3, atol=1e-3 * abs(gx))
+
+
+def test_mirror_field_and_eye_error():
+    """rapt_gb300.utils.Bm (|B| from the device) against the closed dipole form
+    dipoleBm at the Earth dipole's equator, and flutils.eye_error as the
+    difference of the field-line and dipole-form invariants."""
+    import rapt_gb300 as R
+    fld = R.fields.EarthDipole()
+    for L, pa in ((3.0, 30.0), (5.5, 60.0), (7.0, 85.0)):
+        tpos = np.array([0.0, L * Re, 0.0, 0.0])
+        assert abs(R.utils.Bm(tpos, pa, fld) / R.utils.dipoleBm(L, pa) - 1) < 1e-12, (L, pa)
+    rows = GOLD["eye"][(GOLD["eye"][:, 0] == 0) & np.isfinite(GOLD["eye"][:, 4])]
+    for mid, L, eqpa, Bm, ref, dip in rows:
+        tpos = np.array([0.0, L * Re, 0.0, 0.0])
+        err = R.flutils.eye_error(tpos, fld, Bm)
+        want = R.flutils.eye(tpos, fld, Bm) - R.flutils.eye(tpos, fld, Bm, usedipole=True)
+        assert err == want and abs(err) <= 2e-5 * ref + 1e-11 * dip, (err, want, ref, dip)
