@@ -55,7 +55,9 @@ enum { RAPT_KIND_PARTICLE = 0, RAPT_KIND_GC = 1, RAPT_KIND_ADAPTIVE = 2 };
 /* Arithmetic forms. */
 enum {
   RAPT_FORM_PLAIN = 0,        /* FP64 throughout, reference controller semantics */
-  RAPT_FORM_FP32 = 1,         /* FP32 stages, compensated accumulation, FP64 control */
+  RAPT_FORM_FP32 = 1,         /* FP32 stages, compensated accumulation, FP64 control; guiding
+                                 centres: FP32 stencil differences, position tolerance floored
+                                 at 3e-9 of a step's displacement */
   RAPT_FORM_LEARNED = 2,      /* FP64 with MLP step proposals */
   RAPT_FORM_LEARNED_FP32 = 3  /* FP32 stages with MLP step proposals */
 };
