@@ -47,4 +47,5 @@ from . import fields, workloads  # noqa: E402
 from .ensemble import Ensemble  # noqa: E402
 from . import utils  # noqa: E402
 from . import flutils  # noqa: E402
+from .flutils import eye, gradI, halfbouncepath  # noqa: E402,F401  (rapt/__init__.py:42)
 from .tracers import Adaptive, BounceCenter, GuidingCenter, Particle, advance_batch  # noqa: E402
